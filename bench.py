@@ -1,0 +1,369 @@
+"""Benchmark of the smart-interpolation path on one GB300 (or N replicas).
+
+A step is one complete smart interpolation of the all-axis workload —
+uint8 (z, y, x) = (400, 512, 512), 8 phases, labels 0..8 on every 8th XY and
+every 16th YZ/XZ slice, nbrw=10, sorw=4000, smooth=100 — on device-resident
+inputs: label analysis, working image, seed extraction, the walk, argmax,
+100 smoothing iterations per label and the smoothed argmax.
+
+Metric: walker-steps/s = (seeds * nbrw * sorw) / step time (whole job).
+``e2e`` is the same metric through ``smart_interpolation`` with numpy inputs
+and outputs (host->device copies and result download inside the timed region).
+``roofline`` covers the walker kernel (the dominant kernel).
+``--impl reference`` times the reference's own CPU walker on the host cores.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                       [--workload allaxis|plain|large]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    "allaxis": dict(desc="allaxis uint8 (z,y,x)=(400,512,512), 8 phases, labels every 8th XY + every 16th YZ/XZ "
+                         "slice, nbrw=10, sorw=4000, smooth=100", nbrw=10, sorw=4000, smooth=100, allaxis=True),
+    "plain": dict(desc="plain uint8 128^3, 2 ellipsoids, labels every 10th z-slice, nbrw=10, sorw=4000, smooth=0",
+                  nbrw=10, sorw=4000, smooth=0, allaxis=False),
+    "large": dict(desc="large uint8 1024^3, 6 phases, labels every 12th z-slice, nbrw=10, sorw=4000, smooth=100",
+                  nbrw=10, sorw=4000, smooth=100, allaxis=False),
+}
+
+WALK_BYTES_L2 = 192  # 5 gathered 32-B sectors + 1 atomic sector per walker step (uint8 volume)
+WALK_BYTES_PAYLOAD_U8 = 10  # 6 neighbour bytes + one 4-byte hit per step
+
+
+def make_inputs(name: str, seed: int = 0):
+    from biomedisa_gb300 import synthetic as S
+
+    cache = Path(os.environ.get("SI_BENCH_CACHE", "/tmp")) / f"si_bench_{name}_{seed}.npz"
+    if cache.exists():
+        z = np.load(cache)
+        return z["img"], z["lab"]
+    if name == "allaxis":
+        img, lab, _ = S.allaxis_volume(seed=seed)
+    elif name == "plain":
+        img, lab, _ = S.plain_volume(seed=seed)
+    else:
+        img, lab, _ = S.large_volume(seed=seed)
+    try:
+        np.savez(cache, img=img, lab=lab)
+    except OSError:
+        pass
+    return img, lab
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.lines: list[str] = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def flush_l2(buf):
+    buf.add_(1)
+
+
+def run_job(img_t, img_code, lab_t, lab_code, wl, events=None):
+    from biomedisa_gb300.interpolation import DeviceJob
+
+    job = DeviceJob(img_t, img_code, lab_t, lab_code, nbrw=wl["nbrw"], sorw=wl["sorw"], allaxis=wl["allaxis"],
+                    smooth=wl["smooth"])
+    msg = job.analyze()
+    if msg:
+        raise RuntimeError(msg)
+    job.prepare()
+    if events:
+        events[0].record()
+    job.walk()
+    if events:
+        events[1].record()
+    res = job.post()
+    return job, res
+
+
+def cpu_baseline(img, lab, wl, target_seconds):
+    """The reference's OpenCL walker compiled as C on a bounded sample of this
+    workload (same crop/working image the reference would walk)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    import ref_baseline
+
+    labelData, all_labels = oracle.pre_processing(lab)
+    data = np.pad(oracle.normalize_image(img), 1)
+    labelData = np.pad(labelData, 1)
+    az, bz, ay, by, ax, bx = oracle.predict_blocksize(labelData)
+    data = np.ascontiguousarray(data[az:bz, ay:by, ax:bx])
+    labc = np.ascontiguousarray(labelData[az:bz, ay:by, ax:bx])
+    zs = oracle.read_labeled_slices(labc)[0] if not wl["allaxis"] else \
+        [k for k, _ in oracle.read_indices_allx(labc, 0)]
+    z = zs[len(zs) // 2]
+    return ref_baseline.bounded_sample(data, labc, all_labels, z, wl["nbrw"], wl["sorw"], target_seconds)
+
+
+def run_reference(args, wl):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    img, lab = make_inputs(args.workload)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(img, lab, wl, args.ref_seconds)
+        if i >= args.warmup:
+            vals.append(cb)
+    v = statistics.median(c["value"] for c in vals)
+    secs = sum(c["seconds"] for c in vals) / len(vals)
+    line = {
+        "metric": "walker-steps/s", "value": v, "unit": "walker-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": wl["desc"], "global_batch": 1, "parallelism": "host cores"},
+        "cpu_baseline": {"value": v, "unit": "walker-steps/s", "cores": vals[-1]["cores"], "kind": "reference",
+                         "sample": vals[-1]["sample"]},
+        "e2e": {"value": v, "unit": "walker-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="allaxis", choices=sorted(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+        return
+
+    import torch
+
+    from biomedisa_gb300 import interpolation as I
+    from biomedisa_gb300 import smart_interpolation
+
+    world, rank, local = dist_setup()
+    img, lab = make_inputs(args.workload)
+    data, labels = I.normalize_host_dtypes(img, lab)
+    img_code, lab_code = I._IMG_DTYPES[data.dtype], I._LAB_DTYPES[labels.dtype]
+    img_t, lab_t = I.upload(data, labels)
+    torch.cuda.synchronize()
+    l2buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    for _ in range(args.warmup):
+        run_job(img_t, img_code, lab_t, lab_code, wl)
+    torch.cuda.synchronize()
+
+    stream = torch.cuda.current_stream()
+    t_steps, t_walk, launches, steps_per_job = [], [], 0, 0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush_l2(l2buf)
+            torch.cuda.synchronize()
+            barrier(world)
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            ev[2].record(stream)
+            job, _ = run_job(img_t, img_code, lab_t, lab_code, wl, events=ev[:2])
+            ev[3].record(stream)
+            torch.cuda.synchronize()
+            barrier(world)
+            t_steps.append(ev[2].elapsed_time(ev[3]))
+            t_walk.append(ev[0].elapsed_time(ev[1]))
+            launches += job.launches
+            steps_per_job = job.total_steps()
+    ms = max_over_ranks(world, sum(t_steps) / len(t_steps))
+    value = world * steps_per_job / (ms / 1e3)
+    walk_ms = sum(t_walk) / len(t_walk)
+    walk_rate = steps_per_job / (walk_ms / 1e3)
+
+    # end to end through the public API (host numpy in, numpy out)
+    e2e_steps = args.e2e_steps or args.steps
+    smart_interpolation(img, lab, nbrw=wl["nbrw"], sorw=wl["sorw"], allaxis=wl["allaxis"], smooth=wl["smooth"])
+    torch.cuda.synchronize()
+    t_e2e = []
+    out_bytes = 0
+    for _ in range(e2e_steps):
+        flush_l2(l2buf)
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        r = smart_interpolation(img, lab, nbrw=wl["nbrw"], sorw=wl["sorw"], allaxis=wl["allaxis"],
+                                smooth=wl["smooth"])
+        torch.cuda.synchronize()
+        t_e2e.append(time.perf_counter() - t0)
+        out_bytes = sum(v.nbytes for v in r.values())
+    e2e_s = max_over_ranks(world, sum(t_e2e) / len(t_e2e))
+    e2e_value = world * steps_per_job / e2e_s
+
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
+    l2_gbs = measure_l2_gbs(torch)
+    achieved_payload = walk_rate * WALK_BYTES_PAYLOAD_U8 / 1e9
+    achieved_l2 = walk_rate * WALK_BYTES_L2 / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "walker_traffic.json"
+    if tp.exists():
+        tj = json.loads(tp.read_text())
+        traffic = tj.get("dram_bytes_per_step", 0) * steps_per_job if tj.get("workload") == args.workload else None
+
+    line = {
+        "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u8", "data": "synthetic (seeded generator, no public dataset)",
+        "config": {"workload": wl["desc"], "global_batch": 1, "parallelism": f"replicas x{world}" if world > 1
+                   else "single GPU", "l2": "256 MiB buffer written before every timed step; hit maps 3.8 GB > L2"},
+        "voxels_per_s": world * int(np.prod(img.shape)) / (ms / 1e3),
+        "walk_ms": walk_ms, "walk_steps_per_s": walk_rate, "total_walker_steps": steps_per_job,
+        "e2e": {"value": e2e_value, "unit": "walker-steps/s", "seconds": e2e_s,
+                "h2d_bytes_per_step": int(img.nbytes + lab.nbytes), "d2h_bytes_per_step": int(out_bytes)},
+        "gpu_launches": launches // max(args.steps, 1),
+        "roofline": {"bound": "hbm", "achieved": achieved_payload, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved_payload / hbm, "traffic": traffic,
+                     "note": f"walker kernel; algorithmic bytes = {WALK_BYTES_PAYLOAD_U8} B/step logical payload "
+                             f"(6 neighbour bytes + 4-byte hit) x {steps_per_job} steps / CUDA-event duration; "
+                             f"peak {peak_kind}"},
+        "roofline_l2": {"bound": "l2", "achieved": achieved_l2, "peak": l2_gbs, "unit": "GB/s",
+                        "frac": achieved_l2 / l2_gbs if l2_gbs else None,
+                        "note": f"{WALK_BYTES_L2} B/step (5 gather sectors + 1 atomic sector); peak = L2-resident "
+                                "32 MiB device copy measured in this run"},
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = dict(kind="reference", **{k: v for k, v in cpu_baseline(
+                img, lab, wl, args.ref_seconds).items() if k in ("value", "unit", "cores", "sample")})
+        except Exception as e:  # baseline unavailable must not hide the GPU number
+            line["cpu_baseline"] = {"value": None, "unit": "walker-steps/s", "cores": 0, "kind": "reference",
+                                    "sample": f"unavailable: {e}"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def measure_l2_gbs(torch):
+    """L2-resident device copy bandwidth (read + write bytes), best of 20."""
+    a = torch.empty(16 << 20, dtype=torch.uint8, device="cuda")
+    b = torch.empty_like(a)
+    for _ in range(5):
+        b.copy_(a)
+    best = 0.0
+    for _ in range(20):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(50):
+            b.copy_(a)
+        e.record()
+        torch.cuda.synchronize()
+        best = max(best, 50 * 2 * a.numel() / (s.elapsed_time(e) / 1e3) / 1e9)
+    return best
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,83 @@
+"""ctypes binding of libsmartinterp.so (declared in include/smartinterp.h).
+
+The library is required: importing this module without it raises, so no code
+path can silently fall back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libsmartinterp.so"
+
+SI_U8, SI_I8, SI_U16, SI_I16, SI_I32, SI_F32 = range(6)
+
+_c_void_p = ctypes.c_void_p
+_c_int = ctypes.c_int
+_c_u64 = ctypes.c_uint64
+_c_u32 = ctypes.c_uint32
+_c_float = ctypes.c_float
+
+# name -> argtypes (all return int status unless noted)
+_SIGNATURES = {
+    "si_label_histogram": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_void_p],
+    "si_slice_flags": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_int, _c_void_p, _c_void_p, _c_void_p,
+                       _c_void_p, _c_void_p],
+    "si_image_minmax": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_void_p],
+    "si_prepare_image": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int,
+                         _c_float, _c_float, _c_int, _c_void_p, _c_void_p],
+    "si_extract_seeds": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int,
+                         _c_void_p, _c_void_p, _c_void_p, _c_int, _c_void_p, _c_int, _c_void_p, _c_void_p, _c_void_p,
+                         _c_void_p],
+    "si_walk": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_void_p, _c_u32, _c_int, _c_int, _c_u64,
+                _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_argmax": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int,
+                  _c_void_p, _c_void_p, _c_void_p, _c_void_p],
+    "si_remap_labels": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p,
+                        _c_void_p, _c_int, _c_void_p],
+    "si_smooth": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
+}
+
+EXPORTED = ("si_version", "si_last_error", *_SIGNATURES)
+
+
+class NativeError(RuntimeError):
+    """A libsmartinterp entry point returned an error status."""
+
+
+def load(path: Path | str | None = None) -> ctypes.CDLL:
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(
+            f"{p} is missing: build it with `python -m biomedisa_gb300.build` (nvcc, sm_103a). "
+            "There is no CPU fallback."
+        )
+    lib = ctypes.CDLL(str(p))
+    lib.si_version.restype = _c_int
+    lib.si_version.argtypes = []
+    lib.si_last_error.restype = ctypes.c_char_p
+    lib.si_last_error.argtypes = []
+    for name, args in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = _c_int
+        fn.argtypes = args
+    return lib
+
+
+_lib: ctypes.CDLL | None = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = load()
+    return _lib
+
+
+def call(name: str, *args) -> None:
+    """Calls an entry point and raises NativeError on a non-zero status."""
+    L = lib()
+    rc = getattr(L, name)(*args)
+    if rc != 0:
+        msg = L.si_last_error().decode(errors="replace")
+        raise NativeError(f"{name} failed ({rc}): {msg}")

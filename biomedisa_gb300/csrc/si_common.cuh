@@ -1,0 +1,108 @@
+// Shared device definitions for the smart-interpolation kernels.
+//
+// Arithmetic in this file is written with explicit round-to-nearest intrinsics
+// (__fadd_rn, __fmul_rn, __fmaf_rn) so that every result is a fixed sequence of
+// IEEE-754 binary32 operations. The CPU oracle restates the same sequence and
+// must reproduce the integer hit maps bit for bit.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace si {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 counter-based generator.
+// Published method: J. Salmon, M. Moraes, R. Dror, D. Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3", SC'11. Ten rounds of the Philox S-box with the
+// key bumped by the Weyl constants between rounds.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kPhiloxM0 = 0xD2511F53u;
+constexpr uint32_t kPhiloxM1 = 0xCD9E8D57u;
+constexpr uint32_t kPhiloxW0 = 0x9E3779B9u;
+constexpr uint32_t kPhiloxW1 = 0xBB67AE85u;
+
+struct U4 {
+  uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += kPhiloxW0;
+      k1 += kPhiloxW1;
+    }
+    const uint32_t hi0 = __umulhi(kPhiloxM0, c.x);
+    const uint32_t lo0 = kPhiloxM0 * c.x;
+    const uint32_t hi1 = __umulhi(kPhiloxM1, c.z);
+    const uint32_t lo1 = kPhiloxM1 * c.z;
+    c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+  }
+  return c;
+}
+
+// Uniform float in [0, 1) from the top 24 bits of a Philox word (exact).
+__device__ __forceinline__ float u01_from_bits(uint32_t bits) {
+  return __fmul_rn(__uint2float_rn(bits >> 8), 5.9604644775390625e-8f);  // 2^-24
+}
+
+// ---------------------------------------------------------------------------
+// Edge weight w = 2^(-d2 * c), with c = log2(e) / (2 var) per seed, i.e. the
+// Gaussian intensity weight exp(-(B-I)^2 / (2 var)) of the reference walker
+// (biomedisa/features/random_walk/pycuda_small.py:133-136), evaluated by our own
+// method instead of the CUDA math library:
+//   y = d2*c; k = nearest integer to y (round-to-nearest by adding 1.5*2^23);
+//   f = y - k in [-0.5, 0.5]; 2^-f by a degree-5 polynomial fitted to 2^x on
+//   [-0.5, 0.5] (Chebyshev-node least squares, max rel. error 3e-7 in binary32
+//   Horner form); scale by 2^-k through the exponent field.
+// Weights with y >= 125 (exp(-86.6) ~ 2.4e-38) are flushed to zero so the
+// result is always a normal number or exactly zero.
+// ---------------------------------------------------------------------------
+constexpr float kLog2e = 1.44269502162933349609375f;  // binary32 nearest log2(e)
+constexpr float kRoundMagic = 12582912.0f;              // 1.5 * 2^23
+constexpr float kWeightYMax = 125.0f;
+constexpr float kP1 = 0.6931470036506653f;   // 0x3f317215
+constexpr float kP2 = 0.2402222454547882f;   // 0x3e75fcd2
+constexpr float kP3 = 0.055507123470306396f; // 0x3d635b70
+constexpr float kP4 = 0.009670175611972809f; // 0x3c1e6fa8
+constexpr float kP5 = 0.0013260921696200967f;// 0x3aadd045
+
+__device__ __forceinline__ float edge_weight(float d2, float c) {
+  const float y = __fmul_rn(d2, c);
+  if (!(y < kWeightYMax)) return 0.0f;
+  const float r = __fadd_rn(y, kRoundMagic);
+  const float kf = __fsub_rn(r, kRoundMagic);
+  const float g = __fsub_rn(kf, y);  // = -(y - k), exact
+  float p = __fmaf_rn(kP5, g, kP4);
+  p = __fmaf_rn(p, g, kP3);
+  p = __fmaf_rn(p, g, kP2);
+  p = __fmaf_rn(p, g, kP1);
+  p = __fmaf_rn(p, g, 1.0f);
+  const int k = __float_as_int(r) - 0x4B400000;
+  return __int_as_float(__float_as_int(p) - (k << 23));
+}
+
+// Per-seed weight constant c = RN(RN(1 / RN(2 var)) * log2e).
+__device__ __forceinline__ float weight_constant(float var) {
+  const float div1 = __fdiv_rn(1.0f, __fmul_rn(2.0f, var));
+  return __fmul_rn(div1, kLog2e);
+}
+
+// ---------------------------------------------------------------------------
+// One walker start point. pos is the linear index in the working (cropped,
+// padded) volume; c is the weight constant; b is the seed intensity.
+// meta: bits 0-7 label slot, bits 8-9 seed axis, bits 16-23 label value.
+// ---------------------------------------------------------------------------
+struct __align__(16) SeedRec {
+  uint32_t pos;
+  float c;
+  float b;
+  uint32_t meta;
+};
+
+__host__ __device__ __forceinline__ uint32_t seed_slot(uint32_t meta) { return meta & 0xFFu; }
+__host__ __device__ __forceinline__ uint32_t seed_axis(uint32_t meta) { return (meta >> 8) & 0x3u; }
+__host__ __device__ __forceinline__ uint32_t seed_label(uint32_t meta) { return (meta >> 16) & 0xFFu; }
+
+}  // namespace si

@@ -1,0 +1,172 @@
+/*
+ * smartinterp.h — C ABI of the GB300 smart-interpolation library
+ * (libsmartinterp.so, built from biomedisa_gb300/csrc).
+ *
+ * Every entry point takes DEVICE pointers (allocated by the caller), plain
+ * sizes and a cudaStream_t passed as void*. Calls are asynchronous on that
+ * stream; the return value only reports launch/argument errors:
+ *   0 = success, non-zero = error code, message via si_last_error().
+ * No entry point allocates memory unless stated.
+ *
+ * The sequence smart_interpolation() runs is:
+ *   si_label_histogram -> (host: label set) -> si_slice_flags -> (host: crop,
+ *   slice lists) -> si_image_minmax (non-uint8 input only) -> si_prepare_image
+ *   -> si_extract_seeds -> si_walk -> si_argmax -> si_remap_labels
+ *   [-> si_smooth -> si_argmax -> si_remap_labels]
+ */
+#ifndef SMARTINTERP_H
+#define SMARTINTERP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Element types of caller-supplied volumes. */
+enum si_dtype {
+  SI_U8 = 0,
+  SI_I8 = 1,
+  SI_U16 = 2,
+  SI_I16 = 3,
+  SI_I32 = 4,
+  SI_F32 = 5
+};
+
+/* Error codes. */
+enum si_status {
+  SI_OK = 0,
+  SI_ERR_ARG = 1,    /* invalid argument (null pointer, bad size, bad dtype) */
+  SI_ERR_CUDA = 2,   /* CUDA launch error */
+  SI_ERR_LIMIT = 3   /* size beyond a documented limit */
+};
+
+/* One walker start voxel (16 bytes). pos: linear index in the working
+ * (cropped, padded) volume; c: per-seed weight constant log2(e)/(2 var);
+ * b: seed intensity; meta: bits 0-7 label slot, 8-9 seed axis,
+ * 16-23 label value. */
+typedef struct {
+  uint32_t pos;
+  float c;
+  float b;
+  uint32_t meta;
+} si_seed_t;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int si_version(void);
+
+/* Message of the last error raised by this thread ("" if none). */
+const char* si_last_error(void);
+
+/* Histogram of label values. hist[0..255] counts values 0..255, hist[256]
+ * counts negative values, hist[257] values > 255. hist must be zeroed by the
+ * caller. Replaces the label-set scan of pre_processing
+ * (biomedisa/features/biomedisa_helper.py:671 `unique(bm.labelData)`,
+ * :82-103). dtype: SI_U8, SI_I16 or SI_I32. */
+int si_label_histogram(const void* labels, int dtype, uint64_t n,
+                       unsigned long long* hist, void* stream);
+
+/* Labelled-slice flags and bounding box of nonzero labels on the zero-padded
+ * frame (dims Z0+2, Y0+2, X0+2) without materialising the pad.
+ * nz_lut[v] (v = 0..255) is 1 iff value v is nonzero after pre-processing;
+ * negative values count as nonzero, values > 255 as zero.
+ * allaxis = 0: flags_z[k] = 1 iff padded z-slice k holds a nonzero label
+ *   (biomedisa_helper.py:1015-1022 read_labeled_slices).
+ * allaxis = 1: flags_{z,y,x}[k] = 1 iff slice k of that axis keeps a nonzero
+ *   pixel after removing one-pixel-wide lines (the gradient test of
+ *   read_indices_allx / read_labeled_slices_allx, biomedisa_helper.py:1024-1066).
+ * bbox[6] = (zmin, zmax, ymin, ymax, xmin, xmax) in padded coordinates; the
+ * caller initialises it to (INT_MAX, -1, INT_MAX, -1, INT_MAX, -1)
+ * (predict_blocksize before the +-100 margin, biomedisa_helper.py:1105-1116).
+ * flags arrays are zeroed by the caller; flags_y/flags_x may be NULL when
+ * allaxis = 0. */
+int si_slice_flags(const void* labels, int dtype, int Z0, int Y0, int X0,
+                   const uint8_t* nz_lut, int allaxis, uint8_t* flags_z,
+                   uint8_t* flags_y, uint8_t* flags_x, int32_t* bbox,
+                   void* stream);
+
+/* mm[0] = min, mm[1] = max of an image converted to float32 (used for the
+ * [0,255] normalisation of non-uint8 input, biomedisa/interpolation.py:140-144).
+ * The caller initialises mm to (+inf, -inf). dtype: SI_U16, SI_I16, SI_F32. */
+int si_image_minmax(const void* img, int dtype, uint64_t n, float* mm,
+                    void* stream);
+
+/* Working image: the crop [cz0,cz0+Zc) x [cy0,..) x [cx0,..) of the image
+ * padded by one zero voxel on every side (biomedisa/interpolation.py:157 and
+ * :203), after the reference's dtype normalisation (:136-144) and optional
+ * 3x3x3 box denoise (biomedisa_helper.py:308-323).
+ * dtype SI_U8 / SI_I8 -> work is uint8 (int8 shifted by +128);
+ * other dtypes -> work is float32 ((x - norm_min) / norm_range * 255).
+ * Crop coordinates are in the padded frame. */
+int si_prepare_image(const void* img, int dtype, int Z0, int Y0, int X0,
+                     int cz0, int cy0, int cx0, int Zc, int Yc, int Xc,
+                     float norm_min, float norm_range, int denoise,
+                     void* work, void* stream);
+
+/* Seed extraction: every interior voxel of the listed slices whose
+ * (pre-processed) label has a slot becomes one seed, with its in-slice 3x3
+ * same-label variance (pycuda_small.py:114-131; pycuda_small_allx.py:86-105).
+ * slice_list holds n_slices pairs (axis, index in crop coordinates).
+ * slot_lut[v] = label slot of value v (0..255) or -1; values > 255 use
+ * slot_lut[0]; negative values never seed. slot_label[s] = label value of slot s.
+ * row_counts: scratch of n_slices * max(Zc, Yc) + 1 uint32.
+ * seeds: capacity for every interior pixel of the listed slices.
+ * *n_seeds (device) receives the count. Seeds are ordered by
+ * (slice_list entry, row, column). Replaces the seed selection inside the
+ * walker kernels (pycuda_small.py:140-171) and the slice reader
+ * (biomedisa_helper.py:1015-1045). */
+int si_extract_seeds(const void* labels, int dtype, int Z0, int Y0, int X0,
+                     int cz0, int cy0, int cx0, int Zc, int Yc, int Xc,
+                     const int16_t* slot_lut, const uint8_t* slot_label,
+                     const void* work, int work_is_float,
+                     const int32_t* slice_list, int n_slices,
+                     uint32_t* row_counts, si_seed_t* seeds,
+                     uint32_t* n_seeds, void* stream);
+
+/* Random walker. For every seed, nbrw walks of sorw steps; a move into the
+ * interior adds one hit to hits[slot][z][y][x] (uint32, caller-zeroed,
+ * nol * Zc*Yc*Xc). Direction weights, border rule and walk reset follow
+ * pycuda_small.py:138-257; randomness is Philox4x32-10 keyed by `key` with
+ * counter (step/4, seed pos, seed axis, label value).
+ * order 0: walk-major work order (all seeds' walk 0 first), 1: seed-major.
+ * grid/block <= 0 select defaults. max_seeds bounds *n_seeds.
+ * Replaces Funktion/randomWalk and the per-label launch loop
+ * (pycuda_small.py:102-108, pyopencl_small.py:128-134). */
+int si_walk(const void* work, int work_is_float, int Zc, int Yc, int Xc,
+            const si_seed_t* seeds, const uint32_t* n_seeds,
+            uint32_t max_seeds, int nbrw, int sorw, uint64_t key,
+            uint32_t* hits, int nol, int grid, int block, int order,
+            void* stream);
+
+/* Per-voxel argmax over nol maps ([nol][Zc][Yc][Xc], uint32 hits or float32
+ * smoothed maps), first maximum wins (np.argmax, rw_small.py:200). The label
+ * index is written to out (original frame Z0 x Y0 x X0, uint8, caller-zeroed)
+ * at the crop region minus the one-voxel pad (rw_small.py:214-216);
+ * presence[8] (caller-zeroed) receives a bit per index seen.
+ * uq (nullable, same frame as out) receives the uncertainty
+ * uint8(255 * (1 - (1 - m0/m2)(1 - m1/m2))) of the three largest values on the
+ * crop interior and 0 on its border (gpu_kernels.py:54-116, rw_small.py:152-176). */
+int si_argmax(const void* maps, int maps_are_float, int nol, int Zc, int Yc,
+              int Xc, int cz0, int cy0, int cx0, int Z0, int Y0, int X0,
+              uint8_t* out, uint32_t* presence, uint8_t* uq, void* stream);
+
+/* Replace label indices in out (crop region) by label values as get_labels
+ * does (biomedisa_helper.py:1209-1213): index k -> all_labels[k], except the
+ * smallest index present, which maps to 0. */
+int si_remap_labels(uint8_t* out, int Zc, int Yc, int Xc, int cz0, int cy0,
+                    int cx0, int Z0, int Y0, int X0, const uint32_t* presence,
+                    const uint8_t* all_labels, int nol, void* stream);
+
+/* Curvature smoothing (rw_small.py:114-137, gpu_kernels.py:118-183): for each
+ * of the nol maps, iters steps of phi <- phi + 0.01 * kappa(phi) on the
+ * interior, borders unchanged. maps holds uint32 hits on entry and float32
+ * smoothed values (bit pattern) on exit. tmp0/tmp1: float32 scratch of
+ * Zc*Yc*Xc each. */
+int si_smooth(uint32_t* maps, float* tmp0, float* tmp1, int nol, int Zc,
+              int Yc, int Xc, int iters, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SMARTINTERP_H */

@@ -1,0 +1,158 @@
+"""Imports modules of the reference (biomedisa) in this container — TEST
+INFRASTRUCTURE ONLY, used by the oracle's extraction recipe and by the
+golden-fixture generator; never imported by the product or on the GPU host.
+
+The reference's third-party dependencies are missing here, so they are
+replaced by stubs while importing:
+  * ``pycuda.compiler.SourceModule`` and ``pyopencl.Program`` record the
+    kernel source strings they are given (no compilation);
+  * ``numba.jit`` returns the undecorated Python function;
+  * every other missing module is an empty placeholder.
+Nothing under the reference tree is written (bytecode writing is disabled).
+"""
+from __future__ import annotations
+
+import importlib
+import sys
+import types
+from contextlib import contextmanager
+
+REFERENCE_ROOT = "/root/reference"
+
+RECORDED_SOURCES: list[str] = []
+
+
+class _Anything(types.ModuleType):
+    """Placeholder module: any attribute is another placeholder callable."""
+
+    def __getattr__(self, name):
+        if name.startswith("__"):
+            raise AttributeError(name)
+        return _AnyCallable()
+
+
+class _AnyCallable:
+    def __call__(self, *a, **k):
+        return _AnyCallable()
+
+    def __getattr__(self, name):
+        return _AnyCallable()
+
+
+class _SourceModule:
+    def __init__(self, code, *a, **k):
+        RECORDED_SOURCES.append(code)
+        self.code = code
+
+    def get_function(self, name):
+        return _AnyCallable()
+
+
+class _Program:
+    def __init__(self, ctx, code):
+        RECORDED_SOURCES.append(code)
+        self.code = code
+
+    def build(self, *a, **k):
+        return _AnyCallable()
+
+
+def _numba_typed(f):
+    """Runs a numba-compiled function as Python with numba's scalar typing
+    where plain Python/NumPy-2 typing differs: smooth_img_3x3
+    (biomedisa_helper.py:308-323) starts its accumulator at the integer 0,
+    which numba types as int64 (float64 once a float is added); under NumPy 2
+    rules a Python 0 plus a uint8 scalar stays uint8 and overflows. The input
+    is widened to int64/float64 for the call and the result cast back to the
+    input dtype, as numba's store into the uint8/float32 output does."""
+    if getattr(f, "__name__", "") != "smooth_img_3x3":
+        return f
+
+    def wrapper(img):
+        import numpy as np
+
+        wide = img.astype(np.float64 if np.issubdtype(img.dtype, np.floating) else np.int64)
+        return f(wide).astype(img.dtype)
+
+    wrapper.__name__ = f.__name__
+    return wrapper
+
+
+def _numba_jit(*args, **kwargs):
+    if len(args) == 1 and callable(args[0]) and not kwargs:
+        return _numba_typed(args[0])
+    return _numba_typed
+
+
+def _stubs():
+    mods = {}
+    pycuda = _Anything("pycuda")
+    compiler = types.ModuleType("pycuda.compiler")
+    compiler.SourceModule = _SourceModule
+    mods.update({
+        "pycuda": pycuda, "pycuda.compiler": compiler, "pycuda.driver": _Anything("pycuda.driver"),
+        "pycuda.gpuarray": _Anything("pycuda.gpuarray"),
+    })
+    pyopencl = _Anything("pyopencl")
+    pyopencl.Program = _Program
+    mods["pyopencl"] = pyopencl
+    mods["pyopencl.array"] = _Anything("pyopencl.array")
+    numba = types.ModuleType("numba")
+    numba.jit = _numba_jit
+    numba.njit = _numba_jit
+    numba.prange = range
+    mods["numba"] = numba
+    for name in ("tifffile", "medpy", "medpy.io", "skimage", "SimpleITK", "PIL", "cv2", "mpi4py",
+                 "importlib_metadata", "netCDF4", "h5py"):
+        try:
+            if name in ("PIL",):
+                raise ImportError
+            importlib.import_module(name)
+        except Exception:
+            mods[name] = _Anything(name)
+    for name in ("biomedisa.features.amira_to_np.amira_helper", "biomedisa.features.nc_reader"):
+        m = types.ModuleType(name)
+        m.amira_to_np = m.np_to_amira = m.nc_to_np = m.np_to_nc = _AnyCallable()
+        mods[name] = m
+    return mods
+
+
+@contextmanager
+def reference_modules():
+    """Context in which ``import biomedisa...`` resolves to the reference."""
+    saved = {k: sys.modules.get(k) for k in list(sys.modules) if k == "biomedisa" or k.startswith("biomedisa.")}
+    for k in saved:
+        del sys.modules[k]
+    stubs = _stubs()
+    old = {k: sys.modules.get(k) for k in stubs}
+    sys.modules.update(stubs)
+    old_path = list(sys.path)
+    old_dwb = sys.dont_write_bytecode
+    sys.dont_write_bytecode = True
+    sys.path.insert(0, REFERENCE_ROOT)
+    try:
+        yield
+    finally:
+        sys.path[:] = old_path
+        sys.dont_write_bytecode = old_dwb
+        for k, v in old.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+        for k in [k for k in sys.modules if k == "biomedisa" or k.startswith("biomedisa.")]:
+            del sys.modules[k]
+        for k, v in saved.items():
+            if v is not None:
+                sys.modules[k] = v
+
+
+def capture(fn, *args):
+    """Calls a reference kernel factory and returns the source it compiled."""
+    RECORDED_SOURCES.clear()
+    ret = fn(*args)
+    if isinstance(ret, str) and not RECORDED_SOURCES:
+        return ret  # factories that return the source instead of compiling it
+    if len(RECORDED_SOURCES) != 1:
+        raise RuntimeError(f"expected one kernel source, got {len(RECORDED_SOURCES)}")
+    return RECORDED_SOURCES[0]

@@ -1,0 +1,44 @@
+"""The C-ABI library loads and exports every entry point the header declares
+(no compute calls: this runs without a GPU)."""
+import re
+
+from conftest import ROOT
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "smartinterp.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\*?(si_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ("si_walk", "si_extract_seeds", "si_argmax", "si_smooth", "si_label_histogram", "si_slice_flags"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    for s in declared_symbols():
+        assert hasattr(native_lib, s), s
+
+
+def test_python_binding_covers_header(native_lib):
+    from biomedisa_gb300 import _native
+
+    assert set(declared_symbols()) == set(_native.EXPORTED)
+
+
+def test_version_and_error_state(native_lib):
+    assert native_lib.si_version() >= 100
+    assert native_lib.si_last_error() == b""
+
+
+def test_argument_errors_without_launch(native_lib):
+    """Null pointers are rejected before any CUDA call."""
+    from biomedisa_gb300 import _native
+
+    rc = native_lib.si_walk(None, 0, 8, 8, 8, None, None, 0, 1, 1, 0, None, 1, 0, 0, 0, None)
+    assert rc == 1
+    assert b"null pointer" in native_lib.si_last_error()
+    rc = native_lib.si_smooth(None, None, None, 1, 4, 4, 4, 1, None)
+    assert rc == 1
+    assert _native.SI_F32 == 5

@@ -1,0 +1,128 @@
+"""Pins the oracle to the REFERENCE (CPU).
+
+The fixtures in tests/golden/ are outputs of the reference itself — its own
+smart_interpolation with its own kernel sources (see make_golden.py). The
+oracle, switched to the reference's randomness and arithmetic
+(mode='reference'), must reproduce every output bit for bit; its host-logic
+restatements must reproduce the reference helpers' outputs."""
+import io
+import contextlib
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import GOLDEN
+
+PIPELINES = sorted(p.stem.replace("ref_pipeline_", "") for p in GOLDEN.glob("ref_pipeline_*.npz"))
+
+
+def _load(name):
+    z = np.load(GOLDEN / f"ref_pipeline_{name}.npz")
+    kw = eval(str(z["kwargs"]))  # a repr'd dict of literals written by make_golden.py
+    return z, kw
+
+
+def test_fixtures_present():
+    assert len(PIPELINES) >= 9
+
+
+@pytest.mark.parametrize("name", PIPELINES)
+def test_oracle_reproduces_reference_pipeline(name):
+    z, kw = _load(name)
+    res = O.smart_interpolation(
+        z["image"], z["labels"], nbrw=kw["nbrw"], sorw=kw["sorw"], smooth_iters=kw.get("smooth", 0),
+        allaxis=kw.get("allaxis", False), uncertainty_map=kw.get("uncertainty", False),
+        return_hits=kw.get("return_hits", False), denoise=kw.get("denoise", False), only=kw.get("only", "all"),
+        ignore=kw.get("ignore", "none"), mode="reference")
+    keys = [k[4:] for k in z.files if k.startswith("out_")]
+    assert "regular" in keys
+    for k in keys:
+        exp = z["out_" + k]
+        got = res[k]
+        assert got.dtype == exp.dtype, k
+        assert np.array_equal(got, exp), f"{name}: {k} differs ({np.count_nonzero(got != exp)} voxels)"
+
+
+@pytest.fixture(scope="module")
+def helpers():
+    return np.load(GOLDEN / "ref_helpers.npz")
+
+
+def test_allaxis_slice_reader(helpers):
+    for i in range(6):
+        arr = helpers[f"allx_in_{i}"]
+        views = (arr, np.ascontiguousarray(np.swapaxes(arr, 0, 1)),
+                 np.ascontiguousarray(np.swapaxes(np.swapaxes(arr, 0, 1), 0, 2)))
+        for ax, a in enumerate(views):
+            idx, data = O.read_labeled_slices_allx(a, ax)
+            assert [k for k, _ in idx] == list(helpers[f"allx_idx_{i}_{ax}"])
+            assert np.array_equal(data, helpers[f"allx_data_{i}_{ax}"])
+            assert [k for k, _ in O.read_indices_allx(a, ax)] == list(helpers[f"allx_ind_{i}_{ax}"])
+        assert O.read_labeled_slices(arr)[0] == list(helpers[f"rls_idx_{i}"])
+        assert list(O.predict_blocksize(np.pad(arr, 1))) == list(helpers[f"bbox_{i}"])
+
+
+def test_get_labels(helpers):
+    labels = np.asarray([0, 5, 9, 200])
+    assert np.array_equal(O.get_labels(helpers["gl_in_noz"], labels), helpers["gl_out_noz"])
+    assert np.array_equal(O.get_labels(helpers["gl_in"], labels), helpers["gl_out"])
+
+
+def test_pre_processing(helpers):
+    for j in range(4):
+        only, ignore = (str(s) for s in helpers[f"pp_opt_{j}"])
+        try:
+            lab, all_labels = O.pre_processing(helpers[f"pp_in_{j}"], only, ignore)
+        except ValueError:
+            continue
+        assert np.array_equal(lab, helpers[f"pp_lab_{j}"])
+        assert np.array_equal(all_labels, helpers[f"pp_all_{j}"])
+
+
+def test_denoise_and_dice(helpers):
+    assert np.array_equal(O.smooth_img_3x3(helpers["den_u8_in"]), helpers["den_u8_out"])
+    assert np.array_equal(O.smooth_img_3x3(helpers["den_f32_in"]).view(np.uint32),
+                          helpers["den_f32_out"].view(np.uint32))
+    assert O.dice_score(helpers["dice_gt"], helpers["dice_rs"]) == float(helpers["dice"])
+
+
+def _ref_available():
+    try:
+        import ref_extract
+
+        return ref_extract.build(extract_if_possible=False) or ref_extract.build()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(not _ref_available(), reason="oracle/_ref (reference kernels compiled as C) not built")
+@pytest.mark.parametrize("seed", [21, 22])
+def test_oracle_reference_mode_matches_reference_kernels_live(seed):
+    """Fresh random case: the reference CUDA walker compiled as C (launched as
+    pycuda_small.py:96-106 launches it) vs the oracle in reference mode."""
+    import ctypes
+
+    import ref_run
+    from biomedisa_gb300.synthetic import plain_volume
+
+    img, lab, _ = plain_volume(seed=seed, shape=(26, 30, 28), z_every=3, semi=(4, 9))
+    data = np.pad(img, 1)
+    l2 = np.pad(lab, 1)
+    _, all_labels = O.pre_processing(l2)
+    idx, stack = O.read_labeled_slices(l2)
+    seeds = O.extract_seeds(data, l2, [(0, k) for k in idx], all_labels)
+    hits = O.walk_c(data, seeds, 2, 45, 0, len(all_labels), rng="ref_mrg", weight="ref_expf",
+                    rng_index=seeds.rng_cuda)
+    lib = ref_run.ref_lib()
+    raw = (data.astype(np.int16) - 128).astype(np.int8)
+    Z, Y, X = data.shape
+    ind = np.asarray(idx, np.int32)
+    st = np.ascontiguousarray(stack, np.int32)
+    for s, seg in enumerate(all_labels):
+        a = np.zeros((Z, Y, X), np.float32)
+        lib.ref_launch_walk(0, X // 32 + 1, Y // 32 + 1, len(idx), int(seg), raw.ctypes.data_as(ctypes.c_void_p),
+                            st.ctypes.data_as(ctypes.c_void_p), a.ctypes.data_as(ctypes.c_void_p), X, Y, Z,
+                            ind.ctypes.data_as(ctypes.c_void_p), 45, 2)
+        assert np.array_equal(a, hits[s].astype(np.float32)), f"label {seg}"
