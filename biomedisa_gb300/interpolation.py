@@ -474,9 +474,13 @@ def walk(data, slices, indices, indices_child, nbrw, sorw, name=None, ctx=None, 
     sl = torch.from_numpy(np.ascontiguousarray(cp.slice_list.reshape(-1))).to(dev) if entries else \
         torch.zeros(2, dtype=torch.int32, device=dev)
     is_float = data.dtype == np.float32
-    nat.call("si_extract_seeds", _ptr(lab_t), nat.SI_I32, Z, Y, X, 1, 1, 1, Z, Y, X,
-             _ptr(torch.from_numpy(slot_lut).to(dev)), _ptr(torch.from_numpy(slot_label).to(dev)), _ptr(img_t),
-             int(is_float), _ptr(sl), len(entries), _ptr(rows), _ptr(seeds), _ptr(n_seeds), _stream())
+    # device copies must stay referenced until the kernels have run: a freed
+    # block can be handed to the next allocation on the same stream
+    slot_lut_t = torch.from_numpy(slot_lut).to(dev)
+    slot_label_t = torch.from_numpy(slot_label).to(dev)
+    nat.call("si_extract_seeds", _ptr(lab_t), nat.SI_I32, Z, Y, X, 1, 1, 1, Z, Y, X, _ptr(slot_lut_t),
+             _ptr(slot_label_t), _ptr(img_t), int(is_float), _ptr(sl), len(entries), _ptr(rows), _ptr(seeds),
+             _ptr(n_seeds), _stream())
     hits = torch.zeros((max(nol, 1), Z, Y, X), dtype=torch.int32, device=dev)
     nat.call("si_walk", _ptr(img_t), int(is_float), Z, Y, X, _ptr(seeds), _ptr(n_seeds), cap, int(nbrw), int(sorw),
              int(rng_seed), _ptr(hits), max(nol, 1), 0, 0, 0, _stream())
