@@ -271,3 +271,73 @@ extern "C" int si_extract_seeds(const void* labels, int dtype, int Z0, int Y0, i
 #undef SI_SEEDS_FOR
   return check_launch("si_extract_seeds");
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free seed extraction.
+//
+// Some callers cannot allocate device memory at the point where they extract
+// seeds: a plug-in living inside a host application whose own allocator has
+// already claimed the GPU's memory pool, or a pipeline that must not call
+// cudaMalloc because it synchronises the whole device. For them this variant
+// keeps the per-row counters of the count/scan/emit passes in a fixed array
+// that is part of the loaded library image instead of a caller buffer; the
+// caller still provides every input and output.
+//
+// Limit: n_slices * max(Zc, Yc) + 1 <= kStaticRowCounters (1,048,576 counters,
+// 4 MiB, held by every GPU that loads the library until the process exits).
+// The first call on a device looks up the array's device address with that
+// device current; make that first call before any stream capture. All calls
+// share the one array: calls whose work overlaps on the GPU (different streams
+// or threads) race on it. The count pass writes every counter the scan and emit
+// passes read, so nothing left over from an earlier call is ever read.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+constexpr unsigned long long kStaticRowCounters = 1ull << 20;
+constexpr int kMaxDevices = 64;
+std::mutex g_static_rows_mu;
+uint32_t* g_static_rows_dev[kMaxDevices] = {};
+}  // namespace
+
+static __device__ __align__(256) uint32_t g_static_row_counts[kStaticRowCounters];
+
+// Device address of g_static_row_counts for the current device (looked up once
+// per device; the host-side name is not a device address).
+static int static_row_counts(uint32_t** out) {
+  int dev = -1;
+  const cudaError_t ge = cudaGetDevice(&dev);
+  if (ge != cudaSuccess) return set_error(SI_ERR_CUDA, "si_extract_seeds_noalloc: cudaGetDevice: %s",
+                                          cudaGetErrorString(ge));
+  if (dev < 0 || dev >= kMaxDevices) return set_error(SI_ERR_LIMIT, "si_extract_seeds_noalloc: device %d", dev);
+  std::lock_guard<std::mutex> lock(g_static_rows_mu);
+  if (!g_static_rows_dev[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_row_counts);
+    if (e != cudaSuccess || !p)
+      return set_error(SI_ERR_CUDA, "si_extract_seeds_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    g_static_rows_dev[dev] = static_cast<uint32_t*>(p);
+  }
+  *out = g_static_rows_dev[dev];
+  return SI_OK;
+}
+
+extern "C" int si_extract_seeds_noalloc(const void* labels, int dtype, int Z0, int Y0, int X0, int cz0, int cy0,
+                                        int cx0, int Zc, int Yc, int Xc, const int16_t* slot_lut,
+                                        const uint8_t* slot_label, const void* work, int work_is_float,
+                                        const int32_t* slice_list, int n_slices, si_seed_t* seeds,
+                                        uint32_t* n_seeds, void* stream) {
+  clear_error();
+  if (n_slices < 0 || Zc < 0 || Yc < 0) return set_error(SI_ERR_ARG, "si_extract_seeds_noalloc: bad sizes");
+  const unsigned long long need = (unsigned long long)n_slices * (unsigned long long)(Zc > Yc ? Zc : Yc) + 1ull;
+  if (need > kStaticRowCounters)
+    return set_error(SI_ERR_LIMIT,
+                     "si_extract_seeds_noalloc: needs %llu row counters (n_slices * max(Zc, Yc) + 1), "
+                     "the static scratch holds %llu; use si_extract_seeds with a caller buffer",
+                     need, kStaticRowCounters);
+  uint32_t* rows = nullptr;
+  const int rc = static_row_counts(&rows);
+  if (rc != SI_OK) return rc;
+  return si_extract_seeds(labels, dtype, Z0, Y0, X0, cz0, cy0, cx0, Zc, Yc, Xc, slot_lut, slot_label, work,
+                          work_is_float, slice_list, n_slices, rows, seeds, n_seeds, stream);
+}

@@ -123,6 +123,25 @@ int si_extract_seeds(const void* labels, int dtype, int Z0, int Y0, int X0,
                      uint32_t* row_counts, si_seed_t* seeds,
                      uint32_t* n_seeds, void* stream);
 
+/* Allocation-free seed extraction. No counterpart in the reference: it serves
+ * callers that cannot allocate device memory when they extract seeds (for
+ * example a plug-in whose host application owns the GPU's memory pool, or a
+ * pipeline that must avoid cudaMalloc's device-wide synchronisation).
+ * Same arguments and results as si_extract_seeds without row_counts: the
+ * counters live in a static device array of 1,048,576 uint32 (4 MiB per GPU
+ * that loads the library, held until exit), so n_slices * max(Zc, Yc) + 1 must
+ * not exceed 1,048,576 (SI_ERR_LIMIT otherwise). The first call on a device
+ * looks up the array's address with that device current; make it before any
+ * stream capture. Calls share the array: calls that overlap on the GPU race.
+ * Allocates nothing. */
+int si_extract_seeds_noalloc(const void* labels, int dtype, int Z0, int Y0,
+                             int X0, int cz0, int cy0, int cx0, int Zc,
+                             int Yc, int Xc, const int16_t* slot_lut,
+                             const uint8_t* slot_label, const void* work,
+                             int work_is_float, const int32_t* slice_list,
+                             int n_slices, si_seed_t* seeds,
+                             uint32_t* n_seeds, void* stream);
+
 /* Random walker. For every seed, nbrw walks of sorw steps; a move into the
  * interior adds one hit to hits[slot][z][y][x] (uint32, caller-zeroed,
  * nol * Zc*Yc*Xc). Direction weights, border rule and walk reset follow
