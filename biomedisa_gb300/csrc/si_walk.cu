@@ -24,16 +24,82 @@ __device__ __forceinline__ uint32_t pick_word(const U4& r, uint32_t sub) {
   return sub == 0u ? r.x : (sub == 1u ? r.y : (sub == 2u ? r.z : r.w));
 }
 
+// ---------------------------------------------------------------------------
+// Packed neighbourhood records. For every interior voxel v of the working
+// volume one record holds the six neighbour intensities in move order
+// (+z, -z, +y, -y, +x, -x), a refusal mask (bit d set when move d would leave
+// [1, dim-2], pycuda_small.py:236) and I[v]. A walker step then reads ONE
+// record instead of gathering six voxels, and needs no coordinates.
+//   uint8 volume: 8 bytes  {n0..n5, mask, I[v]}
+//   float volume: 32 bytes {n0..n5, mask (as bits), I[v]}
+// Records of non-interior voxels are zero and never read.
+// ---------------------------------------------------------------------------
 template <bool kFloat>
-__global__ void __launch_bounds__(256) walk_kernel(const void* __restrict__ work_v, int Zc, int Yc, int Xc,
+__global__ void __launch_bounds__(256) pack_kernel(const void* __restrict__ work_v, int Zc, int Yc, int Xc,
+                                                   void* __restrict__ packed_v) {
+  const uint32_t F = (uint32_t)Yc * (uint32_t)Xc;
+  const uint64_t V = (uint64_t)F * Zc;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < V; i += stride) {
+    const int x = (int)(i % Xc);
+    const uint64_t zy = i / Xc;
+    const int y = (int)(zy % Yc);
+    const int z = (int)(zy / Yc);
+    const bool inner = z > 0 && y > 0 && x > 0 && z < Zc - 1 && y < Yc - 1 && x < Xc - 1;
+    uint32_t mask = 0;
+    if (inner) {
+      mask |= (z + 1 >= Zc - 1) ? 1u : 0u;
+      mask |= (z - 1 <= 0) ? 2u : 0u;
+      mask |= (y + 1 >= Yc - 1) ? 4u : 0u;
+      mask |= (y - 1 <= 0) ? 8u : 0u;
+      mask |= (x + 1 >= Xc - 1) ? 16u : 0u;
+      mask |= (x - 1 <= 0) ? 32u : 0u;
+    }
+    if (kFloat) {
+      const float* img = static_cast<const float*>(work_v);
+      float4* out = static_cast<float4*>(packed_v) + 2 * i;
+      if (inner) {
+        out[0] = make_float4(img[i + F], img[i - F], img[i + Xc], img[i - Xc]);
+        out[1] = make_float4(img[i + 1], img[i - 1], __uint_as_float(mask), img[i]);
+      } else {
+        out[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+        out[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    } else {
+      const uint8_t* img = static_cast<const uint8_t*>(work_v);
+      uint2 r = make_uint2(0u, 0u);
+      if (inner) {
+        r.x = (uint32_t)img[i + F] | ((uint32_t)img[i - F] << 8) | ((uint32_t)img[i + Xc] << 16) |
+              ((uint32_t)img[i - Xc] << 24);
+        r.y = (uint32_t)img[i + 1] | ((uint32_t)img[i - 1] << 8) | (mask << 16) | ((uint32_t)img[i] << 24);
+      }
+      static_cast<uint2*>(packed_v)[i] = r;
+    }
+  }
+}
+
+// Exact float of intensity byte k of a packed word plus 2^23 (the 2^23 cancels
+// against the seed's 2^23 + B): 0x4B0000bb reinterpreted is 2^23 + bb.
+__device__ __forceinline__ float byte_plus_2p23(uint32_t w, uint32_t k) {
+  return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + k));
+}
+
+template <bool kFloat>
+__global__ void __launch_bounds__(256) walk_kernel(const void* __restrict__ packed_v, int Zc, int Yc, int Xc,
                                                    const SeedRec* __restrict__ seeds,
                                                    const uint32_t* __restrict__ n_seeds_ptr, uint32_t max_seeds,
                                                    int nbrw, int sorw, uint32_t k0, uint32_t k1,
                                                    uint32_t* __restrict__ hits, int order) {
+  __shared__ int32_t s_delta[6];
+  const uint32_t F = (uint32_t)Yc * (uint32_t)Xc;
+  if (threadIdx.x < 6) {
+    const int32_t d[6] = {(int32_t)F, -(int32_t)F, Xc, -Xc, 1, -1};
+    s_delta[threadIdx.x] = d[threadIdx.x];
+  }
+  __syncthreads();
   const uint32_t ns = min(*n_seeds_ptr, max_seeds);
   if (ns == 0) return;
   const uint64_t total = (uint64_t)ns * (uint32_t)nbrw;
-  const uint32_t F = (uint32_t)Yc * (uint32_t)Xc;
   const size_t V = (size_t)F * Zc;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t item = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; item < total; item += stride) {
@@ -47,13 +113,9 @@ __global__ void __launch_bounds__(256) walk_kernel(const void* __restrict__ work
     }
     const SeedRec sd = seeds[s];
     uint32_t pos = sd.pos;
-    int z = (int)(pos / F);
-    const uint32_t rem = pos - (uint32_t)z * F;
-    int y = (int)(rem / (uint32_t)Xc);
-    int x = (int)(rem - (uint32_t)y * (uint32_t)Xc);
     const float c = sd.c;
     const float bf = sd.b;
-    const int bi = (int)bf;
+    const float b23 = __fadd_rn(bf, 8388608.0f);  // 2^23 + B, exact for uint8 B
     uint32_t* __restrict__ hl = hits + (size_t)seed_slot(sd.meta) * V;
     const uint32_t axis = seed_axis(sd.meta), label = seed_label(sd.meta);
     uint32_t t = n * (uint32_t)sorw;
@@ -63,24 +125,28 @@ __global__ void __launch_bounds__(256) walk_kernel(const void* __restrict__ work
       if (sub == 0u && st != 0) rr = philox4x32_10(U4{t >> 2, sd.pos, axis, label}, k0, k1);
       const uint32_t bits = pick_word(rr, sub);
       float w0, w1, w2, w3, w4, w5;
+      uint32_t mask;
       if (kFloat) {
-        const float* __restrict__ img = static_cast<const float*>(work_v);
+        const float4* rec = static_cast<const float4*>(packed_v) + 2 * (size_t)pos;
+        const float4 a = rec[0], b = rec[1];
         float d;
-        d = __fsub_rn(bf, img[pos + F]); w0 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(bf, img[pos - F]); w1 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(bf, img[pos + Xc]); w2 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(bf, img[pos - Xc]); w3 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(bf, img[pos + 1]); w4 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(bf, img[pos - 1]); w5 = edge_weight(__fmul_rn(d, d), c);
+        d = __fsub_rn(bf, a.x); w0 = edge_weight(__fmul_rn(d, d), c);
+        d = __fsub_rn(bf, a.y); w1 = edge_weight(__fmul_rn(d, d), c);
+        d = __fsub_rn(bf, a.z); w2 = edge_weight(__fmul_rn(d, d), c);
+        d = __fsub_rn(bf, a.w); w3 = edge_weight(__fmul_rn(d, d), c);
+        d = __fsub_rn(bf, b.x); w4 = edge_weight(__fmul_rn(d, d), c);
+        d = __fsub_rn(bf, b.y); w5 = edge_weight(__fmul_rn(d, d), c);
+        mask = __float_as_uint(b.z);
       } else {
-        const uint8_t* __restrict__ img = static_cast<const uint8_t*>(work_v);
-        int d;
-        d = bi - (int)img[pos + F]; w0 = edge_weight(__int2float_rn(d * d), c);
-        d = bi - (int)img[pos - F]; w1 = edge_weight(__int2float_rn(d * d), c);
-        d = bi - (int)img[pos + Xc]; w2 = edge_weight(__int2float_rn(d * d), c);
-        d = bi - (int)img[pos - Xc]; w3 = edge_weight(__int2float_rn(d * d), c);
-        d = bi - (int)img[pos + 1]; w4 = edge_weight(__int2float_rn(d * d), c);
-        d = bi - (int)img[pos - 1]; w5 = edge_weight(__int2float_rn(d * d), c);
+        const uint2 r = static_cast<const uint2*>(packed_v)[pos];
+        float d;
+        d = __fsub_rn(b23, byte_plus_2p23(r.x, 0)); w0 = edge_weight(__fmul_rn(d, d), c);
+        d = __fsub_rn(b23, byte_plus_2p23(r.x, 1)); w1 = edge_weight(__fmul_rn(d, d), c);
+        d = __fsub_rn(b23, byte_plus_2p23(r.x, 2)); w2 = edge_weight(__fmul_rn(d, d), c);
+        d = __fsub_rn(b23, byte_plus_2p23(r.x, 3)); w3 = edge_weight(__fmul_rn(d, d), c);
+        d = __fsub_rn(b23, byte_plus_2p23(r.y, 0)); w4 = edge_weight(__fmul_rn(d, d), c);
+        d = __fsub_rn(b23, byte_plus_2p23(r.y, 1)); w5 = edge_weight(__fmul_rn(d, d), c);
+        mask = r.y >> 16;
       }
       const float c1 = __fadd_rn(w0, w1);
       const float c2 = __fadd_rn(c1, w2);
@@ -90,18 +156,8 @@ __global__ void __launch_bounds__(256) walk_kernel(const void* __restrict__ work
       const float rnd = __fmul_rn(c5, u01_from_bits(bits));
       int dir = (int)(w0 <= rnd) + (int)(c1 <= rnd) + (int)(c2 <= rnd) + (int)(c3 <= rnd) + (int)(c4 <= rnd);
       if (rnd == 0.0f) dir = 0;
-      const bool plus = (dir & 1) == 0;
-      const int axis_dir = dir >> 1;  // 0: z, 1: y, 2: x
-      const int coord = axis_dir == 0 ? z : (axis_dir == 1 ? y : x);
-      const int hi = (axis_dir == 0 ? Zc : (axis_dir == 1 ? Yc : Xc)) - 2;
-      const bool ok = plus ? (coord < hi) : (coord > 1);
-      if (ok) {
-        const uint32_t step = axis_dir == 0 ? F : (axis_dir == 1 ? (uint32_t)Xc : 1u);
-        const int dc = plus ? 1 : -1;
-        pos = plus ? pos + step : pos - step;
-        if (axis_dir == 0) z += dc;
-        else if (axis_dir == 1) y += dc;
-        else x += dc;
+      if (!((mask >> dir) & 1u)) {
+        pos += (uint32_t)s_delta[dir];
         atomicAdd(&hl[pos], 1u);
       }
     }
@@ -113,11 +169,30 @@ __global__ void __launch_bounds__(256) walk_kernel(const void* __restrict__ work
 
 using namespace si;
 
-extern "C" int si_walk(const void* work, int work_is_float, int Zc, int Yc, int Xc, const si_seed_t* seeds,
+extern "C" int si_pack_neighbours(const void* work, int work_is_float, int Zc, int Yc, int Xc, void* packed,
+                                  void* stream) {
+  clear_error();
+  if (!work || !packed) return set_error(SI_ERR_ARG, "si_pack_neighbours: null pointer");
+  if (Zc < 3 || Yc < 3 || Xc < 3) return set_error(SI_ERR_ARG, "si_pack_neighbours: bad dims");
+  if ((uint64_t)Zc * Yc * Xc > 0xFFFFFFFFull)
+    return set_error(SI_ERR_LIMIT, "si_pack_neighbours: volume above 2^32 voxels");
+  const uint64_t V = (uint64_t)Zc * Yc * Xc;
+  const int block = 256;
+  const uint64_t want = (V + block - 1) / block, cap = (uint64_t)sm_count() * 16;
+  const int grid = (int)(want < cap ? want : cap);
+  cudaStream_t st = as_stream(stream);
+  if (work_is_float)
+    pack_kernel<true><<<grid, block, 0, st>>>(work, Zc, Yc, Xc, packed);
+  else
+    pack_kernel<false><<<grid, block, 0, st>>>(work, Zc, Yc, Xc, packed);
+  return check_launch("si_pack_neighbours");
+}
+
+extern "C" int si_walk(const void* packed, int work_is_float, int Zc, int Yc, int Xc, const si_seed_t* seeds,
                        const uint32_t* n_seeds, uint32_t max_seeds, int nbrw, int sorw, uint64_t key,
                        uint32_t* hits, int nol, int grid, int block, int order, void* stream) {
   clear_error();
-  if (!work || !seeds || !n_seeds || !hits) return set_error(SI_ERR_ARG, "si_walk: null pointer");
+  if (!packed || !seeds || !n_seeds || !hits) return set_error(SI_ERR_ARG, "si_walk: null pointer");
   if (Zc < 3 || Yc < 3 || Xc < 3) return set_error(SI_ERR_ARG, "si_walk: bad dims");
   if ((uint64_t)Zc * Yc * Xc > 0xFFFFFFFFull) return set_error(SI_ERR_LIMIT, "si_walk: volume above 2^32 voxels");
   if (nbrw < 0 || sorw < 0) return set_error(SI_ERR_ARG, "si_walk: negative nbrw/sorw");
@@ -133,10 +208,10 @@ extern "C" int si_walk(const void* work, int work_is_float, int Zc, int Yc, int 
   const SeedRec* sd = reinterpret_cast<const SeedRec*>(seeds);
   cudaStream_t st = as_stream(stream);
   if (work_is_float)
-    walk_kernel<true><<<grid, block, 0, st>>>(work, Zc, Yc, Xc, sd, n_seeds, max_seeds, nbrw, sorw, k0, k1, hits,
+    walk_kernel<true><<<grid, block, 0, st>>>(packed, Zc, Yc, Xc, sd, n_seeds, max_seeds, nbrw, sorw, k0, k1, hits,
                                               order);
   else
-    walk_kernel<false><<<grid, block, 0, st>>>(work, Zc, Yc, Xc, sd, n_seeds, max_seeds, nbrw, sorw, k0, k1, hits,
+    walk_kernel<false><<<grid, block, 0, st>>>(packed, Zc, Yc, Xc, sd, n_seeds, max_seeds, nbrw, sorw, k0, k1, hits,
                                                order);
   return check_launch("si_walk");
 }

@@ -293,12 +293,14 @@ class DeviceJob:
                  _ptr(self.slot_label), _ptr(self.work), int(self.work_is_float), _ptr(sl), n_sl,
                  _ptr(self.row_counts), _ptr(self.seeds), _ptr(self.n_seeds), _stream())
         self.launches += 3
+        self.packed = pack_neighbours(self.work, self.work_is_float, cp.Zc, cp.Yc, cp.Xc)
+        self.launches += 1
 
     def walk(self):
         cp = self.cplan
         nol = self.lplan.nol
         self.hits = torch.zeros((nol, cp.Zc, cp.Yc, cp.Xc), dtype=torch.int32, device=self.dev)
-        nat.call("si_walk", _ptr(self.work), int(self.work_is_float), cp.Zc, cp.Yc, cp.Xc, _ptr(self.seeds),
+        nat.call("si_walk", _ptr(self.packed), int(self.work_is_float), cp.Zc, cp.Yc, cp.Xc, _ptr(self.seeds),
                  _ptr(self.n_seeds), self.seed_capacity, self.nbrw, self.sorw, self.rng_seed, _ptr(self.hits), nol,
                  int(self.walk_grid), int(self.walk_block), int(self.walk_order), _stream())
         self.launches += 1
@@ -347,6 +349,14 @@ class DeviceJob:
 
     def total_steps(self) -> int:
         return int(self.n_seeds.item()) * self.nbrw * self.sorw
+
+
+def pack_neighbours(work: torch.Tensor, is_float: bool, Zc: int, Yc: int, Xc: int) -> torch.Tensor:
+    """Packed neighbourhood records of a working volume (si_pack_neighbours)."""
+    rec = 32 if is_float else 8
+    packed = torch.empty(Zc * Yc * Xc * rec, dtype=torch.uint8, device=work.device)
+    nat.call("si_pack_neighbours", _ptr(work), int(is_float), Zc, Yc, Xc, _ptr(packed), _stream())
+    return packed
 
 
 def upload(data: np.ndarray, labelData: np.ndarray, device=None, pinned=True):
@@ -482,6 +492,7 @@ def walk(data, slices, indices, indices_child, nbrw, sorw, name=None, ctx=None, 
              _ptr(slot_label_t), _ptr(img_t), int(is_float), _ptr(sl), len(entries), _ptr(rows), _ptr(seeds),
              _ptr(n_seeds), _stream())
     hits = torch.zeros((max(nol, 1), Z, Y, X), dtype=torch.int32, device=dev)
-    nat.call("si_walk", _ptr(img_t), int(is_float), Z, Y, X, _ptr(seeds), _ptr(n_seeds), cap, int(nbrw), int(sorw),
+    packed = pack_neighbours(img_t, is_float, Z, Y, X)
+    nat.call("si_walk", _ptr(packed), int(is_float), Z, Y, X, _ptr(seeds), _ptr(n_seeds), cap, int(nbrw), int(sorw),
              int(rng_seed), _ptr(hits), max(nol, 1), 0, 0, 0, _stream())
     return hits[:nol].float().cpu().numpy()

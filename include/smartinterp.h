@@ -11,7 +11,8 @@
  * The sequence smart_interpolation() runs is:
  *   si_label_histogram -> (host: label set) -> si_slice_flags -> (host: crop,
  *   slice lists) -> si_image_minmax (non-uint8 input only) -> si_prepare_image
- *   -> si_extract_seeds -> si_walk -> si_argmax -> si_remap_labels
+ *   -> si_extract_seeds -> si_pack_neighbours -> si_walk -> si_argmax
+ *   -> si_remap_labels
  *   [-> si_smooth -> si_argmax -> si_remap_labels]
  */
 #ifndef SMARTINTERP_H
@@ -142,16 +143,26 @@ int si_extract_seeds_noalloc(const void* labels, int dtype, int Z0, int Y0,
                              int n_slices, si_seed_t* seeds,
                              uint32_t* n_seeds, void* stream);
 
-/* Random walker. For every seed, nbrw walks of sorw steps; a move into the
- * interior adds one hit to hits[slot][z][y][x] (uint32, caller-zeroed,
- * nol * Zc*Yc*Xc). Direction weights, border rule and walk reset follow
- * pycuda_small.py:138-257; randomness is Philox4x32-10 keyed by `key` with
- * counter (step/4, seed pos, seed axis, label value).
+/* Packed neighbourhood records for the walker: for every interior voxel of
+ * the working volume, its six neighbour intensities in move order
+ * (+z, -z, +y, -y, +x, -x), a refusal mask (bit d set when move d would leave
+ * [1, dim-2], pycuda_small.py:236) and its own intensity.
+ * uint8 work -> 8 bytes per voxel; float32 work -> 32 bytes per voxel.
+ * packed: caller buffer of Zc*Yc*Xc records. */
+int si_pack_neighbours(const void* work, int work_is_float, int Zc, int Yc,
+                       int Xc, void* packed, void* stream);
+
+/* Random walker over packed records (si_pack_neighbours). For every seed,
+ * nbrw walks of sorw steps; a move into the interior adds one hit to
+ * hits[slot][z][y][x] (uint32, caller-zeroed, nol * Zc*Yc*Xc). Direction
+ * weights, border rule and walk reset follow pycuda_small.py:138-257;
+ * randomness is Philox4x32-10 keyed by `key` with counter
+ * (step/4, seed pos, seed axis, label value).
  * order 0: walk-major work order (all seeds' walk 0 first), 1: seed-major.
  * grid/block <= 0 select defaults. max_seeds bounds *n_seeds.
  * Replaces Funktion/randomWalk and the per-label launch loop
  * (pycuda_small.py:102-108, pyopencl_small.py:128-134). */
-int si_walk(const void* work, int work_is_float, int Zc, int Yc, int Xc,
+int si_walk(const void* packed, int work_is_float, int Zc, int Yc, int Xc,
             const si_seed_t* seeds, const uint32_t* n_seeds,
             uint32_t max_seeds, int nbrw, int sorw, uint64_t key,
             uint32_t* hits, int nol, int grid, int block, int order,
