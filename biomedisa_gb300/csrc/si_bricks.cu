@@ -1,0 +1,746 @@
+// Brick walker: the random walk of si_walk, reorganised so that every step
+// reads its neighbourhood record from and counts its hit into SHARED memory.
+//
+// The crop is cut into core bricks of 10^3 voxels. A walker is processed by the
+// CTA of the core brick that holds it, inside the 16^3 extended box of that
+// brick (4 voxels of halo below, 2 above): the CTA loads the box's packed
+// neighbourhood records with one TMA tensor copy, counts hits in a shared
+// 16^3 counter array, and the walker advances until it leaves the box or ends
+// its walk. Leaving walkers keep their state (position, step counter) and are
+// re-bucketed for the next round; each round sorts all live walkers by
+// (label slot, core brick) with a counting sort. Hits of a box are flushed to
+// the global uint32 hit maps once per visit; the step that leaves a box adds
+// its hit with a global atomic.
+//
+// Per-step semantics, randomness (Philox counter (t/4, seed pos, axis, label))
+// and hence the integer hit maps are exactly those of si_walk
+// (pycuda_small.py:138-257 semantics): integer sums do not depend on the order
+// in which walkers or steps are processed.
+#include <cuda.h>
+
+#include <cstring>
+#include <mutex>
+
+#include "si_common.cuh"
+#include "si_internal.h"
+
+namespace si {
+namespace {
+
+constexpr int kCore = 10;   // core brick edge
+constexpr int kLo = 4;      // halo below the core (even: TMA x alignment)
+constexpr int kExt = 16;    // extended box edge (kLo + kCore + 2)
+constexpr int kExtVox = kExt * kExt * kExt;
+constexpr int kAdvThreads = 512;
+constexpr uint32_t kChunk = 4096;  // sorted walkers per work ticket
+constexpr int kScanBlock = 1024;   // elements per scan block (256 threads x 4)
+constexpr uint32_t kWaitLimit = 1u << 26;
+
+struct BrickGeom {
+  int Zc, Yc, Xc;
+  int edge;  // brick edge used for bucketing
+  int nbz, nby, nbx;
+  uint32_t nb;   // bricks per label
+  uint32_t F;    // Yc * Xc
+  uint32_t Xp;   // record row pitch (even)
+};
+
+// Walker state: x = position (crop linear index), y = seed index,
+// z = step counter t, w = end of its walk (24 bits) | label slot << 24.
+__device__ __forceinline__ bool live(const uint4& s) { return s.z != (s.w & 0xFFFFFFu); }
+
+__device__ __forceinline__ void coords(const BrickGeom& g, uint32_t pos, int& z, int& y, int& x) {
+  z = (int)(pos / g.F);
+  const uint32_t r = pos - (uint32_t)z * g.F;
+  y = (int)(r / (uint32_t)g.Xc);
+  x = (int)(r - (uint32_t)y * (uint32_t)g.Xc);
+}
+
+__device__ __forceinline__ uint32_t bucket_of(const BrickGeom& g, const uint4& s) {
+  int z, y, x;
+  coords(g, s.x, z, y, x);
+  const uint32_t e = (uint32_t)g.edge;
+  const uint32_t brick = ((uint32_t)z / e * g.nby + (uint32_t)y / e) * g.nbx + (uint32_t)x / e;
+  return (s.w >> 24) * g.nb + brick;
+}
+
+template <bool kFirst>
+__device__ __forceinline__ bool fetch_state(uint64_t i, uint64_t n, const uint4* __restrict__ states,
+                                            const SeedRec* __restrict__ seeds, uint32_t ns, int sorw, uint4& s) {
+  if (i >= n) return false;
+  if (kFirst) {
+    const uint32_t w = (uint32_t)(i / ns);
+    const uint32_t sidx = (uint32_t)(i - (uint64_t)w * ns);
+    const SeedRec sd = seeds[sidx];
+    s = make_uint4(sd.pos, sidx, w * (uint32_t)sorw, ((w + 1u) * (uint32_t)sorw) | (seed_slot(sd.meta) << 24));
+    return true;
+  }
+  s = states[i];
+  return live(s);
+}
+
+// Count (kScatter = false) or scatter (true) live walkers into buckets, with
+// warp aggregation of equal keys.
+template <bool kFirst, bool kScatter>
+__global__ void __launch_bounds__(256) bucket_kernel(const uint4* __restrict__ states_in, uint64_t n,
+                                                     const SeedRec* __restrict__ seeds, uint32_t ns, int sorw,
+                                                     BrickGeom g, uint32_t* __restrict__ counts,
+                                                     const uint32_t* __restrict__ offsets,
+                                                     uint4* __restrict__ states_out) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+    uint4 s;
+    const bool ok = fetch_state<kFirst>(base + lane, n, states_in, seeds, ns, sorw, s);
+    const uint32_t key = ok ? bucket_of(g, s) : 0u;
+    const uint32_t act = __ballot_sync(0xffffffffu, ok);
+    if (ok) {
+      const uint32_t peers = __match_any_sync(act, key);
+      const int leader = __ffs(peers) - 1;
+      const uint32_t cnt = __popc(peers);
+      if (!kScatter) {
+        if (lane == leader) atomicAdd(&counts[key], cnt);
+      } else {
+        uint32_t b = 0;
+        if (lane == leader) b = atomicAdd(&counts[key], cnt);
+        b = __shfl_sync(peers, b, leader);
+        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        states_out[offsets[key] + b + rank] = s;
+      }
+    }
+  }
+}
+
+// Three-phase exclusive scan of n uint32 counts into offsets[0..n], total into
+// offsets[n] and *total.
+__global__ void __launch_bounds__(256) scan_sums_kernel(const uint32_t* __restrict__ in, uint32_t n,
+                                                        uint32_t* __restrict__ sums) {
+  __shared__ uint32_t red[8];
+  const uint32_t b0 = blockIdx.x * kScanBlock;
+  uint32_t v = 0;
+  for (uint32_t i = b0 + threadIdx.x; i < min(b0 + kScanBlock, n); i += blockDim.x) v += in[i];
+  v = __reduce_add_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    sums[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(1024) scan_top_kernel(uint32_t* __restrict__ sums, uint32_t nblocks) {
+  __shared__ uint32_t part[1024];
+  const uint32_t per = (nblocks + 1023) / 1024;
+  const uint32_t beg = threadIdx.x * per, end = min(beg + per, nblocks);
+  uint32_t s = 0;
+  for (uint32_t i = beg; i < end; ++i) s += sums[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const uint32_t v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+  for (uint32_t i = beg; i < end; ++i) {
+    const uint32_t c = sums[i];
+    sums[i] = run;
+    run += c;
+  }
+}
+
+__global__ void __launch_bounds__(256) scan_apply_kernel(const uint32_t* __restrict__ in, uint32_t n,
+                                                         const uint32_t* __restrict__ sums,
+                                                         uint32_t* __restrict__ out, uint32_t* __restrict__ total) {
+  __shared__ uint32_t warp_tot[8];
+  const uint32_t b0 = blockIdx.x * kScanBlock;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // each thread owns 4 consecutive elements
+  const uint32_t i0 = b0 + threadIdx.x * 4;
+  uint32_t v[4];
+  uint32_t tsum = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = (i0 + k < n) ? in[i0 + k] : 0u;
+    tsum += v[k];
+  }
+  uint32_t incl = tsum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  uint32_t wbase = 0;
+  for (int w = 0; w < wid; ++w) wbase += warp_tot[w];
+  uint32_t run = sums[blockIdx.x] + wbase + incl - tsum;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (i0 + k < n) out[i0 + k] = run;
+    run += v[k];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) {
+    out[n] = run;
+    *total = run;
+  }
+}
+
+// Packed records with an even row pitch (TMA needs 16-byte row strides).
+__global__ void __launch_bounds__(256) pack_pitched_kernel(const uint8_t* __restrict__ img, BrickGeom g,
+                                                           uint2* __restrict__ rec) {
+  const uint64_t V = (uint64_t)g.Zc * g.Yc * g.Xp;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < V; i += stride) {
+    const int x = (int)(i % g.Xp);
+    const uint64_t zy = i / g.Xp;
+    const int y = (int)(zy % g.Yc);
+    const int z = (int)(zy / g.Yc);
+    uint2 r = make_uint2(0u, 0u);
+    if (z > 0 && y > 0 && x > 0 && z < g.Zc - 1 && y < g.Yc - 1 && x < g.Xc - 1) {
+      const size_t p = ((size_t)z * g.Yc + y) * g.Xc + x;
+      uint32_t mask = 0;
+      mask |= (z + 1 >= g.Zc - 1) ? 1u : 0u;
+      mask |= (z - 1 <= 0) ? 2u : 0u;
+      mask |= (y + 1 >= g.Yc - 1) ? 4u : 0u;
+      mask |= (y - 1 <= 0) ? 8u : 0u;
+      mask |= (x + 1 >= g.Xc - 1) ? 16u : 0u;
+      mask |= (x - 1 <= 0) ? 32u : 0u;
+      r.x = (uint32_t)img[p + g.F] | ((uint32_t)img[p - g.F] << 8) | ((uint32_t)img[p + g.Xc] << 16) |
+            ((uint32_t)img[p - g.Xc] << 24);
+      r.y = (uint32_t)img[p + 1] | ((uint32_t)img[p - 1] << 8) | (mask << 16) | ((uint32_t)img[p] << 24);
+    }
+    rec[i] = r;
+  }
+}
+
+// ---- TMA / mbarrier helpers (inline PTX) ----
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void tma_load_box(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ float byte_p23(uint32_t w, uint32_t k) {
+  return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + k));
+}
+
+__device__ __forceinline__ uint32_t pick(const U4& r, uint32_t sub) {
+  return sub == 0u ? r.x : (sub == 1u ? r.y : (sub == 2u ? r.z : r.w));
+}
+
+// Advance all sorted live walkers, chunk by chunk (persistent CTAs).
+__global__ void __launch_bounds__(kAdvThreads, 4) brick_advance_kernel(
+    const __grid_constant__ CUtensorMap rec_map, BrickGeom g, uint4* __restrict__ states,
+    const uint32_t* __restrict__ offsets, uint32_t nbt, uint32_t n_live, uint32_t* __restrict__ chunk_ctr, const SeedRec* __restrict__ seeds, uint32_t k0, uint32_t k1,
+    uint32_t* __restrict__ hits, uint32_t* __restrict__ err) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  uint2* s_rec = reinterpret_cast<uint2*>(smem);
+  uint32_t* s_hits = reinterpret_cast<uint32_t*>(smem + kExtVox * sizeof(uint2));
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint32_t s_chunk, s_bucket, s_end, s_next;
+  const int tid = threadIdx.x;
+  const size_t V = (size_t)g.F * g.Zc;
+  if (tid == 0) mbar_init(&s_bar, 1);
+  __syncthreads();
+  uint32_t phase = 0;
+  for (;;) {
+    if (tid == 0) s_chunk = atomicAdd(chunk_ctr, 1u);
+    __syncthreads();
+    const uint64_t c0 = (uint64_t)s_chunk * kChunk;
+    if (c0 >= n_live) break;
+    const uint64_t c1w = c0 + kChunk;
+    const uint32_t c1 = c1w < (uint64_t)n_live ? (uint32_t)c1w : n_live;
+    uint32_t p = (uint32_t)c0;
+    while (p < c1) {
+      if (tid == 0) {
+        // bucket holding sorted position p: last b with offsets[b] <= p
+        uint32_t lo = 0, hi = nbt;  // offsets has nbt + 1 entries, offsets[nbt] = n_live
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (offsets[mid] <= p) lo = mid; else hi = mid;
+        }
+        s_bucket = lo;
+        s_end = min(offsets[lo + 1], c1);
+        s_next = p;
+      }
+      __syncthreads();
+      const uint32_t bucket = s_bucket;
+      const uint32_t seg_end = s_end;
+      const uint32_t slot = bucket / g.nb;
+      const uint32_t brick = bucket - slot * g.nb;
+      const int bx = (int)(brick % (uint32_t)g.nbx);
+      const int by = (int)((brick / (uint32_t)g.nbx) % (uint32_t)g.nby);
+      const int bz = (int)(brick / ((uint32_t)g.nbx * (uint32_t)g.nby));
+      const int ex0 = bx * kCore - kLo, ey0 = by * kCore - kLo, ez0 = bz * kCore - kLo;
+      if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&s_bar, kExtVox * sizeof(uint2));
+        tma_load_box(s_rec, &rec_map, ex0, ey0, ez0, &s_bar);
+      }
+      for (int i = tid; i < kExtVox; i += kAdvThreads) s_hits[i] = 0u;
+      bool done = false;
+      for (uint32_t it = 0; it < kWaitLimit; ++it) {
+        if (mbar_try_wait(&s_bar, phase)) {
+          done = true;
+          break;
+        }
+      }
+      phase ^= 1u;
+      if (__syncthreads_or(!done)) {
+        if (tid == 0) atomicOr(err, 1u);
+        return;
+      }
+      uint32_t* __restrict__ hl = hits + (size_t)slot * V;
+      for (;;) {
+        const uint32_t w = atomicAdd(&s_next, 1u);
+        if (w >= seg_end) break;
+        uint4 st = states[w];
+        const SeedRec sd = seeds[st.y];
+        const float c = sd.c;
+        const float b23 = __fadd_rn(sd.b, 8388608.0f);
+        const uint32_t axis = seed_axis(sd.meta), label = seed_label(sd.meta);
+        int z, y, x;
+        coords(g, st.x, z, y, x);
+        uint32_t l = ((uint32_t)(z - ez0) << 8) | ((uint32_t)(y - ey0) << 4) | (uint32_t)(x - ex0);
+        uint32_t t = st.z;
+        const uint32_t te = st.w & 0xFFFFFFu;
+        uint32_t blk = t >> 2;
+        U4 rr = philox4x32_10(U4{blk, sd.pos, axis, label}, k0, k1);
+        bool left = false;
+        uint32_t gpos = st.x;
+        while (t < te) {
+          if ((t >> 2) != blk) {
+            blk = t >> 2;
+            rr = philox4x32_10(U4{blk, sd.pos, axis, label}, k0, k1);
+          }
+          const uint32_t bits = pick(rr, t & 3u);
+          const uint2 r = s_rec[l];
+          float d, w0, w1, w2, w3, w4, w5;
+          d = __fsub_rn(b23, byte_p23(r.x, 0)); w0 = edge_weight(__fmul_rn(d, d), c);
+          d = __fsub_rn(b23, byte_p23(r.x, 1)); w1 = edge_weight(__fmul_rn(d, d), c);
+          d = __fsub_rn(b23, byte_p23(r.x, 2)); w2 = edge_weight(__fmul_rn(d, d), c);
+          d = __fsub_rn(b23, byte_p23(r.x, 3)); w3 = edge_weight(__fmul_rn(d, d), c);
+          d = __fsub_rn(b23, byte_p23(r.y, 0)); w4 = edge_weight(__fmul_rn(d, d), c);
+          d = __fsub_rn(b23, byte_p23(r.y, 1)); w5 = edge_weight(__fmul_rn(d, d), c);
+          const float c1 = __fadd_rn(w0, w1);
+          const float c2 = __fadd_rn(c1, w2);
+          const float c3 = __fadd_rn(c2, w3);
+          const float c4 = __fadd_rn(c3, w4);
+          const float c5 = __fadd_rn(c4, w5);
+          const float rnd = __fmul_rn(c5, u01_from_bits(bits));
+          int dir = (int)(w0 <= rnd) + (int)(c1 <= rnd) + (int)(c2 <= rnd) + (int)(c3 <= rnd) + (int)(c4 <= rnd);
+          if (rnd == 0.0f) dir = 0;
+          ++t;
+          if ((r.y >> (16 + dir)) & 1u) continue;  // refused: the step counts, nothing is hit
+          const uint32_t shift = (uint32_t)(2 - (dir >> 1)) * 4u;  // z: 8, y: 4, x: 0
+          const uint32_t coord = (l >> shift) & 15u;
+          const bool plus = (dir & 1) == 0;
+          if (plus ? coord == 15u : coord == 0u) {
+            // the move leaves the box: global hit, walker continues next round
+            const int zz = ez0 + (int)(l >> 8) + (dir == 0) - (dir == 1);
+            const int yy = ey0 + (int)((l >> 4) & 15u) + (dir == 2) - (dir == 3);
+            const int xx = ex0 + (int)(l & 15u) + (dir == 4) - (dir == 5);
+            gpos = (uint32_t)zz * g.F + (uint32_t)yy * (uint32_t)g.Xc + (uint32_t)xx;
+            atomicAdd(&hl[gpos], 1u);
+            left = true;
+            break;
+          }
+          l = plus ? l + (1u << shift) : l - (1u << shift);
+          atomicAdd(&s_hits[l], 1u);
+        }
+        st.z = t;
+        if (left) st.x = gpos;
+        states[w] = st;
+      }
+      __syncthreads();
+      // flush the box counters
+      for (int i = tid; i < kExtVox; i += kAdvThreads) {
+        const uint32_t v = s_hits[i];
+        if (v) {
+          const int zz = ez0 + (i >> 8), yy = ey0 + ((i >> 4) & 15), xx = ex0 + (i & 15);
+          atomicAdd(&hl[(size_t)zz * g.F + (size_t)yy * g.Xc + xx], v);
+        }
+      }
+      __syncthreads();
+      p = seg_end;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Sorted sweep: every live walker advances exactly min(K, steps left) steps over
+// the packed records in global memory (uniform work per thread). Walkers are
+// counting-sorted by (label slot, 8^3 brick) between sweeps, so the threads
+// resident at any moment work on a compact slab of the volume and its records
+// and hit counters stay in L2.
+// ---------------------------------------------------------------------------
+template <bool kFloat>
+__global__ void __launch_bounds__(256) sweep_kernel(const void* __restrict__ packed, BrickGeom g,
+                                                    uint4* __restrict__ states, uint32_t n_live, uint32_t K,
+                                                    const SeedRec* __restrict__ seeds, uint32_t k0, uint32_t k1,
+                                                    uint32_t* __restrict__ hits) {
+  __shared__ int32_t s_delta[6];
+  if (threadIdx.x < 6) {
+    const int32_t F = (int32_t)g.F, X = g.Xc;
+    s_delta[threadIdx.x] = threadIdx.x == 0 ? F : threadIdx.x == 1 ? -F : threadIdx.x == 2 ? X
+                           : threadIdx.x == 3 ? -X : threadIdx.x == 4 ? 1 : -1;
+  }
+  __syncthreads();
+  const size_t V = (size_t)g.F * g.Zc;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_live; i += stride) {
+    uint4 st = states[i];
+    const SeedRec sd = seeds[st.y];
+    const uint32_t te = st.w & 0xFFFFFFu;
+    const uint32_t t_end = min(st.z + K, te);
+    uint32_t* __restrict__ hl = hits + (size_t)(st.w >> 24) * V;
+    st.x = walk_steps<kFloat>(packed, st.x, st.z, t_end, sd.c, sd.b, sd.pos, seed_axis(sd.meta),
+                              seed_label(sd.meta), k0, k1, hl, s_delta);
+    st.z = t_end;
+    states[i] = st;
+  }
+}
+
+// ---- host side ----
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+struct ScratchLayout {
+  size_t rec, states0, states1, counts, offsets, sums, ctrs, total;
+};
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+ScratchLayout layout(const BrickGeom& g, uint64_t max_walks, int nol) {
+  ScratchLayout L{};
+  const uint64_t nbt = (uint64_t)g.nb * nol;
+  const uint64_t nblocks = (nbt + kScanBlock - 1) / kScanBlock;
+  size_t off = 0;
+  L.rec = off;
+  off = align_up(off + (size_t)g.Zc * g.Yc * g.Xp * sizeof(uint2), 256);
+  L.states0 = off;
+  off = align_up(off + max_walks * sizeof(uint4), 256);
+  L.states1 = off;
+  off = align_up(off + max_walks * sizeof(uint4), 256);
+  L.counts = off;
+  off = align_up(off + (nbt + 1) * sizeof(uint32_t), 256);
+  L.offsets = off;
+  off = align_up(off + (nbt + 1) * sizeof(uint32_t), 256);
+  L.sums = off;
+  off = align_up(off + (nblocks + 1) * sizeof(uint32_t), 256);
+  L.ctrs = off;  // [0] n_live, [1] chunk counter, [2] error flag
+  off = align_up(off + 4 * sizeof(uint32_t), 256);
+  L.total = off;
+  return L;
+}
+
+BrickGeom make_geom(int Zc, int Yc, int Xc, int edge = kCore) {
+  BrickGeom g{};
+  g.Zc = Zc;
+  g.Yc = Yc;
+  g.Xc = Xc;
+  g.edge = edge;
+  g.nbz = (Zc + edge - 1) / edge;
+  g.nby = (Yc + edge - 1) / edge;
+  g.nbx = (Xc + edge - 1) / edge;
+  g.nb = (uint32_t)g.nbz * g.nby * g.nbx;
+  g.F = (uint32_t)Yc * Xc;
+  g.Xp = (uint32_t)((Xc + 1) & ~1);
+  return g;
+}
+
+int advance_blocks_per_sm() {
+  static int cached = 0;
+  if (!cached) {
+    const int smem = kExtVox * (int)(sizeof(uint2) + sizeof(uint32_t));
+    cudaFuncSetAttribute(brick_advance_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, brick_advance_kernel, kAdvThreads, smem) != cudaSuccess ||
+        n < 1)
+      n = 1;
+    cached = n;
+  }
+  return cached;
+}
+
+}  // namespace
+}  // namespace si
+
+using namespace si;
+
+extern "C" int si_walk_bricks_scratch(int Zc, int Yc, int Xc, uint64_t max_walks, int nol,
+                                      unsigned long long* bytes) {
+  clear_error();
+  if (!bytes || Zc < 3 || Yc < 3 || Xc < 3 || nol < 1 || nol > 256)
+    return set_error(SI_ERR_ARG, "si_walk_bricks_scratch: bad arguments");
+  *bytes = layout(make_geom(Zc, Yc, Xc), max_walks, nol).total;
+  return SI_OK;
+}
+
+extern "C" int si_walk_bricks(const void* work, int Zc, int Yc, int Xc, const si_seed_t* seeds,
+                              const uint32_t* n_seeds, uint32_t max_seeds, int nbrw, int sorw, uint64_t key,
+                              uint32_t* hits, int nol, void* scratch, unsigned long long scratch_bytes,
+                              int* rounds_out, void* stream) {
+  clear_error();
+  if (!work || !seeds || !n_seeds || !hits || !scratch) return set_error(SI_ERR_ARG, "si_walk_bricks: null pointer");
+  if (Zc < 3 || Yc < 3 || Xc < 3 || nol < 1 || nol > 256) return set_error(SI_ERR_ARG, "si_walk_bricks: bad dims");
+  if ((uint64_t)Zc * Yc * Xc > 0xFFFFFFFFull) return set_error(SI_ERR_LIMIT, "si_walk_bricks: volume above 2^32");
+  if (nbrw < 0 || sorw < 0 || (uint64_t)nbrw * (uint64_t)sorw >= (1ull << 24))
+    return set_error(SI_ERR_LIMIT, "si_walk_bricks: nbrw*sorw must be below 2^24");
+  cudaStream_t st = as_stream(stream);
+  if (rounds_out) *rounds_out = 0;
+  uint32_t ns = 0;
+  if (cudaMemcpyAsync(&ns, n_seeds, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return set_error(SI_ERR_CUDA, "si_walk_bricks: reading the seed count failed");
+  ns = ns < max_seeds ? ns : max_seeds;
+  const uint64_t walks = (uint64_t)ns * (uint64_t)nbrw;
+  if (walks == 0 || sorw == 0) return SI_OK;
+  if (walks >= 0xFFFFFFFFull) return set_error(SI_ERR_LIMIT, "si_walk_bricks: more than 2^32 walks");
+  const BrickGeom g = make_geom(Zc, Yc, Xc);
+  const ScratchLayout L = layout(g, walks, nol);
+  if (scratch_bytes < L.total)
+    return set_error(SI_ERR_ARG, "si_walk_bricks: scratch of %llu bytes, %llu needed", scratch_bytes,
+                     (unsigned long long)L.total);
+  uint8_t* base = static_cast<uint8_t*>(scratch);
+  uint2* rec = reinterpret_cast<uint2*>(base + L.rec);
+  uint4* states[2] = {reinterpret_cast<uint4*>(base + L.states0), reinterpret_cast<uint4*>(base + L.states1)};
+  uint32_t* counts = reinterpret_cast<uint32_t*>(base + L.counts);
+  uint32_t* offsets = reinterpret_cast<uint32_t*>(base + L.offsets);
+  uint32_t* sums = reinterpret_cast<uint32_t*>(base + L.sums);
+  uint32_t* ctrs = reinterpret_cast<uint32_t*>(base + L.ctrs);
+  const uint32_t nbt = g.nb * (uint32_t)nol;
+  const uint32_t nblocks = (nbt + kScanBlock - 1) / kScanBlock;
+  const SeedRec* sd = reinterpret_cast<const SeedRec*>(seeds);
+
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return set_error(SI_ERR_CUDA, "si_walk_bricks: cuTensorMapEncodeTiled unavailable");
+  CUtensorMap map;
+  std::memset(&map, 0, sizeof(map));
+  const cuuint64_t dims[3] = {(cuuint64_t)g.Xc, (cuuint64_t)g.Yc, (cuuint64_t)g.Zc};
+  const cuuint64_t strides[2] = {(cuuint64_t)g.Xp * sizeof(uint2), (cuuint64_t)g.Xp * g.Yc * sizeof(uint2)};
+  const cuuint32_t box[3] = {kExt, kExt, kExt};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult cr = enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, rec, dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) return set_error(SI_ERR_CUDA, "si_walk_bricks: tensor map encoding failed (%d)", (int)cr);
+
+  const int sms = sm_count();
+  const int gb = sms * 8;
+  pack_pitched_kernel<<<sms * 16, 256, 0, st>>>(static_cast<const uint8_t*>(work), g, rec);
+  if (cudaMemsetAsync(ctrs, 0, 4 * sizeof(uint32_t), st) != cudaSuccess)
+    return set_error(SI_ERR_CUDA, "si_walk_bricks: memset failed");
+  const int smem = kExtVox * (int)(sizeof(uint2) + sizeof(uint32_t));
+  const int adv_grid = sms * advance_blocks_per_sm();
+  const uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
+  int cur = 0;
+  int rounds = 0;
+  uint64_t n_prev = walks;  // entries of the previous round (round 0: virtual (seed, walk) pairs)
+  for (;; ++rounds) {
+    const bool first = rounds == 0;
+    if (cudaMemsetAsync(counts, 0, (size_t)(nbt + 1) * sizeof(uint32_t), st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_walk_bricks: memset failed");
+    if (first)
+      bucket_kernel<true, false><<<gb, 256, 0, st>>>(nullptr, n_prev, sd, ns, sorw, g, counts, nullptr, nullptr);
+    else
+      bucket_kernel<false, false><<<gb, 256, 0, st>>>(states[cur], n_prev, sd, ns, sorw, g, counts, nullptr,
+                                                      nullptr);
+    scan_sums_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums);
+    scan_top_kernel<<<1, 1024, 0, st>>>(sums, nblocks);
+    scan_apply_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums, offsets, ctrs);
+    uint32_t live_now = 0;
+    if (cudaMemcpyAsync(&live_now, ctrs, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_walk_bricks: round %d: %s", rounds, cudaGetErrorString(cudaGetLastError()));
+    if (live_now == 0) break;
+    if (cudaMemsetAsync(counts, 0, (size_t)(nbt + 1) * sizeof(uint32_t), st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_walk_bricks: memset failed");
+    const int nxt = first ? 0 : 1 - cur;
+    if (first)
+      bucket_kernel<true, true><<<gb, 256, 0, st>>>(nullptr, n_prev, sd, ns, sorw, g, counts, offsets, states[nxt]);
+    else
+      bucket_kernel<false, true><<<gb, 256, 0, st>>>(states[cur], n_prev, sd, ns, sorw, g, counts, offsets,
+                                                     states[nxt]);
+    cur = nxt;
+    if (cudaMemsetAsync(ctrs + 1, 0, sizeof(uint32_t), st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_walk_bricks: memset failed");
+    brick_advance_kernel<<<adv_grid, kAdvThreads, smem, st>>>(map, g, states[cur], offsets, nbt, live_now, ctrs + 1,
+                                                               sd, k0, k1, hits, ctrs + 2);
+    const int rc = check_launch("si_walk_bricks: advance");
+    if (rc) return rc;
+    n_prev = live_now;
+    if (rounds > 100000) return set_error(SI_ERR_LIMIT, "si_walk_bricks: no convergence");
+  }
+  uint32_t err = 0;
+  if (cudaMemcpyAsync(&err, ctrs + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return set_error(SI_ERR_CUDA, "si_walk_bricks: final sync failed");
+  if (err) return set_error(SI_ERR_CUDA, "si_walk_bricks: a TMA wait timed out");
+  if (rounds_out) *rounds_out = rounds;
+  return check_launch("si_walk_bricks");
+}
+
+namespace si {
+namespace {
+constexpr int kSortEdge = 8;
+
+struct SortLayout {
+  size_t states0, states1, counts, offsets, sums, ctrs, total;
+};
+
+SortLayout sort_layout(const BrickGeom& g, uint64_t max_walks, int nol) {
+  SortLayout L{};
+  const uint64_t nbt = (uint64_t)g.nb * nol;
+  const uint64_t nblocks = (nbt + kScanBlock - 1) / kScanBlock;
+  size_t off = 0;
+  L.states0 = off;
+  off = align_up(off + max_walks * sizeof(uint4), 256);
+  L.states1 = off;
+  off = align_up(off + max_walks * sizeof(uint4), 256);
+  L.counts = off;
+  off = align_up(off + (nbt + 1) * sizeof(uint32_t), 256);
+  L.offsets = off;
+  off = align_up(off + (nbt + 1) * sizeof(uint32_t), 256);
+  L.sums = off;
+  off = align_up(off + (nblocks + 1) * sizeof(uint32_t), 256);
+  L.ctrs = off;
+  off = align_up(off + 4 * sizeof(uint32_t), 256);
+  L.total = off;
+  return L;
+}
+}  // namespace
+}  // namespace si
+
+extern "C" int si_walk_sorted_scratch(int Zc, int Yc, int Xc, uint64_t max_walks, int nol,
+                                      unsigned long long* bytes) {
+  clear_error();
+  if (!bytes || Zc < 3 || Yc < 3 || Xc < 3 || nol < 1 || nol > 256)
+    return set_error(SI_ERR_ARG, "si_walk_sorted_scratch: bad arguments");
+  *bytes = sort_layout(make_geom(Zc, Yc, Xc, kSortEdge), max_walks, nol).total;
+  return SI_OK;
+}
+
+extern "C" int si_walk_sorted(const void* packed, int work_is_float, int Zc, int Yc, int Xc,
+                              const si_seed_t* seeds, const uint32_t* n_seeds, uint32_t max_seeds, int nbrw,
+                              int sorw, uint64_t key, uint32_t* hits, int nol, int sweep_steps, void* scratch,
+                              unsigned long long scratch_bytes, int* rounds_out, void* stream) {
+  clear_error();
+  if (!packed || !seeds || !n_seeds || !hits || !scratch) return set_error(SI_ERR_ARG, "si_walk_sorted: null pointer");
+  if (Zc < 3 || Yc < 3 || Xc < 3 || nol < 1 || nol > 256) return set_error(SI_ERR_ARG, "si_walk_sorted: bad dims");
+  if ((uint64_t)Zc * Yc * Xc > 0xFFFFFFFFull) return set_error(SI_ERR_LIMIT, "si_walk_sorted: volume above 2^32");
+  if (nbrw < 0 || sorw < 0 || (uint64_t)nbrw * (uint64_t)sorw >= (1ull << 24))
+    return set_error(SI_ERR_LIMIT, "si_walk_sorted: nbrw*sorw must be below 2^24");
+  if (sweep_steps <= 0) sweep_steps = 64;
+  cudaStream_t st = as_stream(stream);
+  if (rounds_out) *rounds_out = 0;
+  uint32_t ns = 0;
+  if (cudaMemcpyAsync(&ns, n_seeds, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return set_error(SI_ERR_CUDA, "si_walk_sorted: reading the seed count failed");
+  ns = ns < max_seeds ? ns : max_seeds;
+  const uint64_t walks = (uint64_t)ns * (uint64_t)nbrw;
+  if (walks == 0 || sorw == 0) return SI_OK;
+  if (walks >= 0xFFFFFFFFull) return set_error(SI_ERR_LIMIT, "si_walk_sorted: more than 2^32 walks");
+  const BrickGeom g = make_geom(Zc, Yc, Xc, kSortEdge);
+  const SortLayout L = sort_layout(g, walks, nol);
+  if (scratch_bytes < L.total)
+    return set_error(SI_ERR_ARG, "si_walk_sorted: scratch of %llu bytes, %llu needed", scratch_bytes,
+                     (unsigned long long)L.total);
+  uint8_t* base = static_cast<uint8_t*>(scratch);
+  uint4* states[2] = {reinterpret_cast<uint4*>(base + L.states0), reinterpret_cast<uint4*>(base + L.states1)};
+  uint32_t* counts = reinterpret_cast<uint32_t*>(base + L.counts);
+  uint32_t* offsets = reinterpret_cast<uint32_t*>(base + L.offsets);
+  uint32_t* sums = reinterpret_cast<uint32_t*>(base + L.sums);
+  uint32_t* ctrs = reinterpret_cast<uint32_t*>(base + L.ctrs);
+  const uint32_t nbt = g.nb * (uint32_t)nol;
+  const uint32_t nblocks = (nbt + kScanBlock - 1) / kScanBlock;
+  const SeedRec* sd = reinterpret_cast<const SeedRec*>(seeds);
+  const int sms = sm_count();
+  const int gb = sms * 8;
+  const uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
+  int cur = 0, rounds = 0;
+  uint64_t n_prev = walks;
+  for (;; ++rounds) {
+    const bool first = rounds == 0;
+    if (cudaMemsetAsync(counts, 0, (size_t)(nbt + 1) * sizeof(uint32_t), st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_walk_sorted: memset failed");
+    if (first)
+      bucket_kernel<true, false><<<gb, 256, 0, st>>>(nullptr, n_prev, sd, ns, sorw, g, counts, nullptr, nullptr);
+    else
+      bucket_kernel<false, false><<<gb, 256, 0, st>>>(states[cur], n_prev, sd, ns, sorw, g, counts, nullptr,
+                                                      nullptr);
+    scan_sums_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums);
+    scan_top_kernel<<<1, 1024, 0, st>>>(sums, nblocks);
+    scan_apply_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums, offsets, ctrs);
+    uint32_t live_now = 0;
+    if (cudaMemcpyAsync(&live_now, ctrs, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_walk_sorted: round %d: %s", rounds, cudaGetErrorString(cudaGetLastError()));
+    if (live_now == 0) break;
+    if (cudaMemsetAsync(counts, 0, (size_t)(nbt + 1) * sizeof(uint32_t), st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_walk_sorted: memset failed");
+    const int nxt = first ? 0 : 1 - cur;
+    if (first)
+      bucket_kernel<true, true><<<gb, 256, 0, st>>>(nullptr, n_prev, sd, ns, sorw, g, counts, offsets, states[nxt]);
+    else
+      bucket_kernel<false, true><<<gb, 256, 0, st>>>(states[cur], n_prev, sd, ns, sorw, g, counts, offsets,
+                                                     states[nxt]);
+    cur = nxt;
+    const uint64_t want_blocks = ((uint64_t)live_now + 255) / 256;
+    const uint32_t blocks = (uint32_t)(want_blocks < (uint64_t)sms * 8 ? want_blocks : (uint64_t)sms * 8);
+    if (work_is_float)
+      sweep_kernel<true><<<blocks, 256, 0, st>>>(packed, g, states[cur], live_now, (uint32_t)sweep_steps, sd, k0, k1,
+                                                 hits);
+    else
+      sweep_kernel<false><<<blocks, 256, 0, st>>>(packed, g, states[cur], live_now, (uint32_t)sweep_steps, sd, k0,
+                                                  k1, hits);
+    const int rc = check_launch("si_walk_sorted: sweep");
+    if (rc) return rc;
+    n_prev = live_now;
+    if (rounds > (1 << 24)) return set_error(SI_ERR_LIMIT, "si_walk_sorted: no convergence");
+  }
+  if (rounds_out) *rounds_out = rounds;
+  return check_launch("si_walk_sorted");
+}

@@ -105,4 +105,70 @@ __host__ __device__ __forceinline__ uint32_t seed_slot(uint32_t meta) { return m
 __host__ __device__ __forceinline__ uint32_t seed_axis(uint32_t meta) { return (meta >> 8) & 0x3u; }
 __host__ __device__ __forceinline__ uint32_t seed_label(uint32_t meta) { return (meta >> 16) & 0xFFu; }
 
+// ---------------------------------------------------------------------------
+// Walker steps t in [t, t_end) from voxel pos over packed neighbourhood
+// records (8-byte uint8 records or 32-byte float records, see si_walk.cu).
+// Returns the final position. s_delta[d]: linear offset of move d.
+// Semantics: pycuda_small.py:183-253 (weights, cumulative intervals, rnd == 0
+// -> +z, refused border moves count as steps, one hit per accepted move).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float byte_plus_2p23(uint32_t w, uint32_t k) {
+  return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + k));
+}
+
+template <bool kFloat>
+__device__ __forceinline__ uint32_t walk_steps(const void* __restrict__ packed_v, uint32_t pos, uint32_t t,
+                                               uint32_t t_end, float c, float bf, uint32_t seed_pos,
+                                               uint32_t axis, uint32_t label, uint32_t k0, uint32_t k1,
+                                               uint32_t* __restrict__ hl, const int32_t* s_delta) {
+  const float b23 = __fadd_rn(bf, 8388608.0f);  // 2^23 + B, exact for uint8 B
+  uint32_t blk = t >> 2;
+  U4 rr = philox4x32_10(U4{blk, seed_pos, axis, label}, k0, k1);
+  for (; t < t_end; ++t) {
+    if ((t >> 2) != blk) {
+      blk = t >> 2;
+      rr = philox4x32_10(U4{blk, seed_pos, axis, label}, k0, k1);
+    }
+    const uint32_t sub = t & 3u;
+    const uint32_t bits = sub == 0u ? rr.x : (sub == 1u ? rr.y : (sub == 2u ? rr.z : rr.w));
+    float w0, w1, w2, w3, w4, w5;
+    uint32_t mask;
+    if (kFloat) {
+      const float4* rec = static_cast<const float4*>(packed_v) + 2 * (size_t)pos;
+      const float4 a = rec[0], b = rec[1];
+      float d;
+      d = __fsub_rn(bf, a.x); w0 = edge_weight(__fmul_rn(d, d), c);
+      d = __fsub_rn(bf, a.y); w1 = edge_weight(__fmul_rn(d, d), c);
+      d = __fsub_rn(bf, a.z); w2 = edge_weight(__fmul_rn(d, d), c);
+      d = __fsub_rn(bf, a.w); w3 = edge_weight(__fmul_rn(d, d), c);
+      d = __fsub_rn(bf, b.x); w4 = edge_weight(__fmul_rn(d, d), c);
+      d = __fsub_rn(bf, b.y); w5 = edge_weight(__fmul_rn(d, d), c);
+      mask = __float_as_uint(b.z);
+    } else {
+      const uint2 r = static_cast<const uint2*>(packed_v)[pos];
+      float d;
+      d = __fsub_rn(b23, byte_plus_2p23(r.x, 0)); w0 = edge_weight(__fmul_rn(d, d), c);
+      d = __fsub_rn(b23, byte_plus_2p23(r.x, 1)); w1 = edge_weight(__fmul_rn(d, d), c);
+      d = __fsub_rn(b23, byte_plus_2p23(r.x, 2)); w2 = edge_weight(__fmul_rn(d, d), c);
+      d = __fsub_rn(b23, byte_plus_2p23(r.x, 3)); w3 = edge_weight(__fmul_rn(d, d), c);
+      d = __fsub_rn(b23, byte_plus_2p23(r.y, 0)); w4 = edge_weight(__fmul_rn(d, d), c);
+      d = __fsub_rn(b23, byte_plus_2p23(r.y, 1)); w5 = edge_weight(__fmul_rn(d, d), c);
+      mask = r.y >> 16;
+    }
+    const float c1 = __fadd_rn(w0, w1);
+    const float c2 = __fadd_rn(c1, w2);
+    const float c3 = __fadd_rn(c2, w3);
+    const float c4 = __fadd_rn(c3, w4);
+    const float c5 = __fadd_rn(c4, w5);
+    const float rnd = __fmul_rn(c5, u01_from_bits(bits));
+    int dir = (int)(w0 <= rnd) + (int)(c1 <= rnd) + (int)(c2 <= rnd) + (int)(c3 <= rnd) + (int)(c4 <= rnd);
+    if (rnd == 0.0f) dir = 0;
+    if (!((mask >> dir) & 1u)) {
+      pos += (uint32_t)s_delta[dir];
+      atomicAdd(&hl[pos], 1u);
+    }
+  }
+  return pos;
+}
+
 }  // namespace si

@@ -78,12 +78,6 @@ __global__ void __launch_bounds__(256) pack_kernel(const void* __restrict__ work
   }
 }
 
-// Exact float of intensity byte k of a packed word plus 2^23 (the 2^23 cancels
-// against the seed's 2^23 + B): 0x4B0000bb reinterpreted is 2^23 + bb.
-__device__ __forceinline__ float byte_plus_2p23(uint32_t w, uint32_t k) {
-  return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + k));
-}
-
 template <bool kFloat>
 __global__ void __launch_bounds__(256) walk_kernel(const void* __restrict__ packed_v, int Zc, int Yc, int Xc,
                                                    const SeedRec* __restrict__ seeds,
@@ -112,55 +106,10 @@ __global__ void __launch_bounds__(256) walk_kernel(const void* __restrict__ pack
       n = (uint32_t)(item - (uint64_t)s * (uint32_t)nbrw);
     }
     const SeedRec sd = seeds[s];
-    uint32_t pos = sd.pos;
-    const float c = sd.c;
-    const float bf = sd.b;
-    const float b23 = __fadd_rn(bf, 8388608.0f);  // 2^23 + B, exact for uint8 B
     uint32_t* __restrict__ hl = hits + (size_t)seed_slot(sd.meta) * V;
-    const uint32_t axis = seed_axis(sd.meta), label = seed_label(sd.meta);
-    uint32_t t = n * (uint32_t)sorw;
-    U4 rr = philox4x32_10(U4{t >> 2, sd.pos, axis, label}, k0, k1);
-    for (int st = 0; st < sorw; ++st, ++t) {
-      const uint32_t sub = t & 3u;
-      if (sub == 0u && st != 0) rr = philox4x32_10(U4{t >> 2, sd.pos, axis, label}, k0, k1);
-      const uint32_t bits = pick_word(rr, sub);
-      float w0, w1, w2, w3, w4, w5;
-      uint32_t mask;
-      if (kFloat) {
-        const float4* rec = static_cast<const float4*>(packed_v) + 2 * (size_t)pos;
-        const float4 a = rec[0], b = rec[1];
-        float d;
-        d = __fsub_rn(bf, a.x); w0 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(bf, a.y); w1 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(bf, a.z); w2 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(bf, a.w); w3 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(bf, b.x); w4 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(bf, b.y); w5 = edge_weight(__fmul_rn(d, d), c);
-        mask = __float_as_uint(b.z);
-      } else {
-        const uint2 r = static_cast<const uint2*>(packed_v)[pos];
-        float d;
-        d = __fsub_rn(b23, byte_plus_2p23(r.x, 0)); w0 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(b23, byte_plus_2p23(r.x, 1)); w1 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(b23, byte_plus_2p23(r.x, 2)); w2 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(b23, byte_plus_2p23(r.x, 3)); w3 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(b23, byte_plus_2p23(r.y, 0)); w4 = edge_weight(__fmul_rn(d, d), c);
-        d = __fsub_rn(b23, byte_plus_2p23(r.y, 1)); w5 = edge_weight(__fmul_rn(d, d), c);
-        mask = r.y >> 16;
-      }
-      const float c1 = __fadd_rn(w0, w1);
-      const float c2 = __fadd_rn(c1, w2);
-      const float c3 = __fadd_rn(c2, w3);
-      const float c4 = __fadd_rn(c3, w4);
-      const float c5 = __fadd_rn(c4, w5);
-      const float rnd = __fmul_rn(c5, u01_from_bits(bits));
-      int dir = (int)(w0 <= rnd) + (int)(c1 <= rnd) + (int)(c2 <= rnd) + (int)(c3 <= rnd) + (int)(c4 <= rnd);
-      if (rnd == 0.0f) dir = 0;
-      if (!((mask >> dir) & 1u)) {
-        pos += (uint32_t)s_delta[dir];
-        atomicAdd(&hl[pos], 1u);
-      }
-    }
+    const uint32_t t0 = n * (uint32_t)sorw;
+    walk_steps<kFloat>(packed_v, sd.pos, t0, t0 + (uint32_t)sorw, sd.c, sd.b, sd.pos, seed_axis(sd.meta),
+                       seed_label(sd.meta), k0, k1, hl, s_delta);
   }
 }
 

@@ -18,6 +18,7 @@ libsmartinterp.so on one GPU. Differences from the reference, by design:
 """
 from __future__ import annotations
 
+import ctypes
 import time
 from dataclasses import dataclass, field
 
@@ -27,6 +28,7 @@ import torch
 from . import _native as nat
 
 DEFAULT_RNG_SEED = 0x243F6A8885A308D3
+WALKERS = ("auto", "sorted", "tiles", "packed")
 SEED_RECORD_BYTES = 16
 
 
@@ -209,7 +211,12 @@ class DeviceJob:
 
     def __init__(self, img: torch.Tensor, img_code: int, lab: torch.Tensor, lab_code: int, *, nbrw=10, sorw=4000,
                  allaxis=False, smooth=0, uncertainty=False, denoise=False, only="all", ignore="none",
-                 rng_seed=DEFAULT_RNG_SEED, walk_grid=0, walk_block=0, walk_order=0):
+                 rng_seed=DEFAULT_RNG_SEED, walk_grid=0, walk_block=0, walk_order=0, walker="auto",
+                 sweep_steps=64):
+        if walker not in WALKERS:
+            raise ValueError(f"walker must be one of {WALKERS}")
+        self.sweep_steps = int(sweep_steps)
+        self.walker = walker
         if img.dim() != 3 or lab.dim() != 3 or tuple(img.shape) != tuple(lab.shape):
             raise ValueError("image and labels must be 3-D volumes of the same shape")
         self.img, self.img_code, self.lab, self.lab_code = img, img_code, lab, lab_code
@@ -293,13 +300,34 @@ class DeviceJob:
                  _ptr(self.slot_label), _ptr(self.work), int(self.work_is_float), _ptr(sl), n_sl,
                  _ptr(self.row_counts), _ptr(self.seeds), _ptr(self.n_seeds), _stream())
         self.launches += 3
-        self.packed = pack_neighbours(self.work, self.work_is_float, cp.Zc, cp.Yc, cp.Xc)
-        self.launches += 1
+        long_walks = self.nbrw * self.sorw >= (1 << 24)
+        kind = self.walker
+        if kind == "auto":
+            kind = "packed" if long_walks else "sorted"
+        if kind == "tiles" and (self.work_is_float or long_walks):
+            raise ValueError("the tile walker needs a uint8 volume and nbrw*sorw < 2^24")
+        if kind == "sorted" and long_walks:
+            raise ValueError("the sorted walker needs nbrw*sorw < 2^24")
+        self.walker_used = kind
+        if kind != "tiles":
+            self.packed = pack_neighbours(self.work, self.work_is_float, cp.Zc, cp.Yc, cp.Xc)
+            self.launches += 1
 
     def walk(self):
         cp = self.cplan
         nol = self.lplan.nol
         self.hits = torch.zeros((nol, cp.Zc, cp.Yc, cp.Xc), dtype=torch.int32, device=self.dev)
+        if self.walker_used == "tiles":
+            self.rounds = walk_bricks(self.work, cp.Zc, cp.Yc, cp.Xc, self.seeds, self.n_seeds, self.seed_capacity,
+                                      self.nbrw, self.sorw, self.rng_seed, self.hits, nol)
+            self.launches += 1 + 9 * self.rounds
+            return
+        if self.walker_used == "sorted":
+            self.rounds = walk_sorted(self.packed, self.work_is_float, cp.Zc, cp.Yc, cp.Xc, self.seeds,
+                                      self.n_seeds, self.seed_capacity, self.nbrw, self.sorw, self.rng_seed,
+                                      self.hits, nol, self.sweep_steps)
+            self.launches += 6 * self.rounds + 4
+            return
         nat.call("si_walk", _ptr(self.packed), int(self.work_is_float), cp.Zc, cp.Yc, cp.Xc, _ptr(self.seeds),
                  _ptr(self.n_seeds), self.seed_capacity, self.nbrw, self.sorw, self.rng_seed, _ptr(self.hits), nol,
                  int(self.walk_grid), int(self.walk_block), int(self.walk_order), _stream())
@@ -359,6 +387,33 @@ def pack_neighbours(work: torch.Tensor, is_float: bool, Zc: int, Yc: int, Xc: in
     return packed
 
 
+def walk_bricks(work, Zc, Yc, Xc, seeds, n_seeds, max_seeds, nbrw, sorw, key, hits, nol) -> int:
+    """Brick walker (si_walk_bricks) with scratch from the caching allocator.
+    Returns the number of rounds."""
+    need = ctypes.c_ulonglong(0)
+    walks = int(max_seeds) * int(nbrw)
+    nat.call("si_walk_bricks_scratch", Zc, Yc, Xc, walks, nol, ctypes.byref(need))
+    scratch = torch.empty(max(int(need.value), 1), dtype=torch.uint8, device=work.device)
+    rounds = ctypes.c_int(0)
+    nat.call("si_walk_bricks", _ptr(work), Zc, Yc, Xc, _ptr(seeds), _ptr(n_seeds), int(max_seeds), int(nbrw),
+             int(sorw), int(key), _ptr(hits), nol, _ptr(scratch), int(need.value), ctypes.byref(rounds), _stream())
+    return int(rounds.value)
+
+
+def walk_sorted(packed, is_float, Zc, Yc, Xc, seeds, n_seeds, max_seeds, nbrw, sorw, key, hits, nol,
+                sweep_steps=64) -> int:
+    """Sorted-sweep walker (si_walk_sorted) with scratch from the caching
+    allocator. Returns the number of sweeps."""
+    need = ctypes.c_ulonglong(0)
+    nat.call("si_walk_sorted_scratch", Zc, Yc, Xc, int(max_seeds) * int(nbrw), nol, ctypes.byref(need))
+    scratch = torch.empty(max(int(need.value), 1), dtype=torch.uint8, device=packed.device)
+    rounds = ctypes.c_int(0)
+    nat.call("si_walk_sorted", _ptr(packed), int(is_float), Zc, Yc, Xc, _ptr(seeds), _ptr(n_seeds), int(max_seeds),
+             int(nbrw), int(sorw), int(key), _ptr(hits), nol, int(sweep_steps), _ptr(scratch), int(need.value),
+             ctypes.byref(rounds), _stream())
+    return int(rounds.value)
+
+
 def upload(data: np.ndarray, labelData: np.ndarray, device=None, pinned=True):
     """Copies host volumes to the device (pinned staging for full H2D speed)."""
     dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -376,7 +431,7 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
                         platform=None, allaxis=False, ignore="none", only="all", smooth=0, compression=True,
                         return_hits=False, img_id=None, label_id=None, remote=False, queue=0, clean=None, fill=None,
                         slicer=False, *, rng_seed=DEFAULT_RNG_SEED, device=None, return_device=False,
-                        walk_grid=0, walk_block=0, walk_order=0):
+                        walk_grid=0, walk_block=0, walk_order=0, walker="auto", sweep_steps=64):
     """Smart interpolation of sparsely pre-segmented slices on one GB300.
 
     Same parameters and result keys as the reference
@@ -384,8 +439,11 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
     'smooth', 'uncertainty', 'hits'). Errors print 'Error: ...' and return
     None as the reference does. ``platform`` is accepted and ignored (one CUDA
     device). Extra keyword-only arguments: ``rng_seed`` (Philox key),
-    ``device``, ``return_device`` (keep results as device tensors) and the
-    walker launch shape (``walk_grid``, ``walk_block``, ``walk_order``).
+    ``device``, ``return_device`` (keep results as device tensors), ``walker``
+    ('auto' = 'sorted': sorted sweeps of ``sweep_steps`` steps; 'tiles':
+    shared-memory brick walker, uint8 only; 'packed': one thread per walk) and
+    the packed walker's launch shape (``walk_grid``, ``walk_block``,
+    ``walk_order``). All walkers give identical hit maps.
     """
     if data is None or labelData is None:
         raise NotImplementedError("loading volumes from files is outside this package; pass numpy arrays")
@@ -404,7 +462,7 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
     job = DeviceJob(img, _IMG_DTYPES[np.dtype(data.dtype)], lab, _LAB_DTYPES[np.dtype(labelData.dtype)], nbrw=nbrw,
                     sorw=sorw, allaxis=allaxis, smooth=smooth, uncertainty=uncertainty, denoise=denoise, only=only,
                     ignore=ignore, rng_seed=rng_seed, walk_grid=walk_grid, walk_block=walk_block,
-                    walk_order=walk_order)
+                    walk_order=walk_order, walker=walker, sweep_steps=sweep_steps)
     msg = job.analyze()
     if msg:
         return _err(msg)
@@ -493,6 +551,10 @@ def walk(data, slices, indices, indices_child, nbrw, sorw, name=None, ctx=None, 
              _ptr(n_seeds), _stream())
     hits = torch.zeros((max(nol, 1), Z, Y, X), dtype=torch.int32, device=dev)
     packed = pack_neighbours(img_t, is_float, Z, Y, X)
-    nat.call("si_walk", _ptr(packed), int(is_float), Z, Y, X, _ptr(seeds), _ptr(n_seeds), cap, int(nbrw), int(sorw),
-             int(rng_seed), _ptr(hits), max(nol, 1), 0, 0, 0, _stream())
+    if int(nbrw) * int(sorw) < (1 << 24):
+        walk_sorted(packed, is_float, Z, Y, X, seeds, n_seeds, cap, int(nbrw), int(sorw), int(rng_seed), hits,
+                    max(nol, 1))
+    else:
+        nat.call("si_walk", _ptr(packed), int(is_float), Z, Y, X, _ptr(seeds), _ptr(n_seeds), cap, int(nbrw),
+                 int(sorw), int(rng_seed), _ptr(hits), max(nol, 1), 0, 0, 0, _stream())
     return hits[:nol].float().cpu().numpy()

@@ -168,6 +168,49 @@ int si_walk(const void* packed, int work_is_float, int Zc, int Yc, int Xc,
             uint32_t* hits, int nol, int grid, int block, int order,
             void* stream);
 
+/* Scratch bytes si_walk_bricks needs for a crop of Zc x Yc x Xc voxels, up
+ * to max_walks walks (seeds * nbrw) and nol labels. */
+int si_walk_bricks_scratch(int Zc, int Yc, int Xc, uint64_t max_walks, int nol,
+                           unsigned long long* bytes);
+
+/* Brick walker: the same walk and the same uint32 hit maps as si_walk, for a
+ * uint8 working volume, computed with every step's neighbourhood record and
+ * hit counter in shared memory. The crop is cut into 10^3 core bricks; a CTA
+ * loads the 16^3 box around a core (TMA tensor copy of packed records) and
+ * advances the walkers of one (label, brick) bucket until they leave the box
+ * or finish; walkers are re-sorted by bucket every round (counting sort) until
+ * none is left. work: uint8 working image (si_prepare_image); scratch: caller
+ * buffer of si_walk_bricks_scratch bytes; rounds_out (nullable) receives the
+ * number of rounds. nbrw * sorw must be below 2^24. Synchronises `stream`
+ * once per round to read the number of live walkers. Replaces the same
+ * reference code as si_walk. */
+int si_walk_bricks(const void* work, int Zc, int Yc, int Xc,
+                   const si_seed_t* seeds, const uint32_t* n_seeds,
+                   uint32_t max_seeds, int nbrw, int sorw, uint64_t key,
+                   uint32_t* hits, int nol, void* scratch,
+                   unsigned long long scratch_bytes, int* rounds_out,
+                   void* stream);
+
+/* Scratch bytes si_walk_sorted needs (crop dims, max walks = seeds * nbrw,
+ * labels). */
+int si_walk_sorted_scratch(int Zc, int Yc, int Xc, uint64_t max_walks, int nol,
+                           unsigned long long* bytes);
+
+/* Sorted-sweep walker: the same walk and the same uint32 hit maps as si_walk
+ * over packed records (si_pack_neighbours), run as sweeps in which every live
+ * walker advances min(sweep_steps, steps left) steps (default 64 when <= 0);
+ * between sweeps the walkers are counting-sorted by (label slot, 8^3 brick),
+ * so concurrently running walkers share a compact, cache-resident part of
+ * the volume and of the hit maps. scratch: si_walk_sorted_scratch bytes;
+ * rounds_out (nullable) receives the number of sweeps. nbrw * sorw must be
+ * below 2^24. Synchronises `stream` once per sweep. */
+int si_walk_sorted(const void* packed, int work_is_float, int Zc, int Yc,
+                   int Xc, const si_seed_t* seeds, const uint32_t* n_seeds,
+                   uint32_t max_seeds, int nbrw, int sorw, uint64_t key,
+                   uint32_t* hits, int nol, int sweep_steps, void* scratch,
+                   unsigned long long scratch_bytes, int* rounds_out,
+                   void* stream);
+
 /* Per-voxel argmax over nol maps ([nol][Zc][Yc][Xc], uint32 hits or float32
  * smoothed maps), first maximum wins (np.argmax, rw_small.py:200). The label
  * index is written to out (original frame Z0 x Y0 x X0, uint8, caller-zeroed)

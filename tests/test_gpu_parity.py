@@ -22,6 +22,8 @@ def _cases():
     img, lab, truth = plain_volume(seed=1, shape=(40, 36, 34), z_every=5, semi=(6, 12))
     base = dict(nbrw=3, sorw=70, smooth=3, uncertainty=True, return_hits=True)
     yield "u8", img, lab, base
+    yield "u8_packed_walker", img, lab, dict(base, walker="packed")
+    yield "u8_tiles_walker", img, lab, dict(base, walker="tiles")
     yield "u16", img.astype(np.uint16) * 3 + 7, lab, base
     yield "i8_denoise", (img.astype(np.int16) - 128).astype(np.int8), lab, dict(base, denoise=True, smooth=0)
     yield "f32_denoise", img.astype(np.float32) * 0.37 - 5.0, lab, dict(base, denoise=True, smooth=2)
@@ -42,6 +44,7 @@ def _cases():
     img3, _, truth3 = plain_volume(seed=4, shape=(38, 40, 36), z_every=6, semi=(7, 13))
     lab3 = sparse_labels(truth3.astype(np.int32), z_every=6, y_every=9, x_every=9)
     yield "allaxis_u8", img3, lab3, dict(base, allaxis=True, smooth=2)
+    yield "allaxis_u8_packed", img3, lab3, dict(base, allaxis=True, smooth=0, walker="packed")
     yield "allaxis_u16", img3.astype(np.uint16) * 5, lab3, dict(base, allaxis=True, smooth=0)
     # labels near the volume border (crop clamped), odd sizes
     img4, _, truth4 = plain_volume(seed=9, shape=(17, 23, 29), z_every=2, semi=(4, 9))
@@ -108,14 +111,32 @@ def test_seeds_and_plans_bit_exact(allaxis, cuda):
 
 
 def test_walk_invariant_to_launch_shape(cuda):
+    """Packed walker under several launch shapes and work orders, and the brick
+    walker, give the same hit maps."""
     img, lab, _ = plain_volume(seed=13, shape=(44, 40, 42), z_every=5, semi=(7, 13))
-    ref = None
+    ref = smart_interpolation(img, lab, nbrw=2, sorw=50, return_hits=True, walker="tiles")["hits"]
+    assert ref.sum() > 0
+    for k in (1, 7, 64, 1000):
+        r = smart_interpolation(img, lab, nbrw=2, sorw=50, return_hits=True, walker="sorted", sweep_steps=k)
+        assert np.array_equal(r["hits"], ref)
     for grid, block, order in ((0, 0, 0), (7, 64, 0), (152, 256, 1), (1, 32, 1)):
         r = smart_interpolation(img, lab, nbrw=2, sorw=50, return_hits=True, walk_grid=grid, walk_block=block,
-                                walk_order=order)
-        if ref is None:
-            ref = r["hits"]
+                                walk_order=order, walker="packed")
         assert np.array_equal(r["hits"], ref)
+
+
+@pytest.mark.parametrize("shape,sorw", [((23, 31, 29), 300), ((12, 70, 9), 500), ((64, 48, 56), 120)])
+@pytest.mark.parametrize("walker", ["tiles", "sorted"])
+def test_brick_walkers_long_walks_bit_exact(shape, sorw, walker, cuda):
+    """Walks much longer than a brick or a sweep (many rounds, odd crop sizes,
+    x extent below one brick): tile and sorted walkers == oracle."""
+    img, lab, _ = plain_volume(seed=sum(shape), shape=shape, z_every=3, semi=(3, 9))
+    key = 77
+    got = smart_interpolation(img, lab, nbrw=2, sorw=sorw, return_hits=True, rng_seed=key, walker=walker,
+                              sweep_steps=37)
+    exp = O.smart_interpolation(img, lab, nbrw=2, sorw=sorw, return_hits=True, key=key)
+    assert np.array_equal(got["hits"], exp["hits"])
+    assert np.array_equal(got["regular"], exp["regular"])
 
 
 def test_walk_plugin_seam_matches_oracle(cuda):
