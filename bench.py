@@ -41,7 +41,7 @@ WORKLOADS = {
                   nbrw=10, sorw=4000, smooth=100, allaxis=False),
 }
 
-WALK_BYTES_L2 = 192  # 5 gathered 32-B sectors + 1 atomic sector per walker step (uint8 volume)
+WALK_SECTORS_L2 = 2  # per walker step at L2: one packed-record sector + one atomic sector
 WALK_BYTES_PAYLOAD_U8 = 10  # 6 neighbour bytes + one 4-byte hit per step
 
 
@@ -231,8 +231,21 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-jobs", type=int, default=0,
+                    help="run this many untimed jobs and exit (for ncu captures; no JSON line)")
+    ap.add_argument("--nbrw", type=int, default=None, help="override (profiling only)")
+    ap.add_argument("--sorw", type=int, default=None, help="override (profiling only)")
+    ap.add_argument("--smooth", type=int, default=None, help="override (profiling only)")
     args = ap.parse_args()
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    for k in ("nbrw", "sorw", "smooth"):
+        if getattr(args, k) is not None:
+            if not args.profile_jobs:
+                ap.error(f"--{k} is only allowed with --profile-jobs")
+            wl[k] = getattr(args, k)
+    if args.profile_jobs:
+        profile_jobs(args, wl)
+        return
     if args.impl == "reference":
         run_reference(args, wl)
         return
@@ -301,9 +314,10 @@ def main():
         peaks = json.loads(pk.read_text())
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
-    l2_gbs = measure_l2_gbs(torch)
+    l2 = measure_l2(torch)
+    l2_gbs = l2["read_gbs"]
     achieved_payload = walk_rate * WALK_BYTES_PAYLOAD_U8 / 1e9
-    achieved_l2 = walk_rate * WALK_BYTES_L2 / 1e9
+    achieved_l2 = walk_rate * WALK_SECTORS_L2 * 32 / 1e9
     traffic = None
     tp = ROOT / "profiles" / "walker_traffic.json"
     if tp.exists():
@@ -328,8 +342,10 @@ def main():
                              f"peak {peak_kind}"},
         "roofline_l2": {"bound": "l2", "achieved": achieved_l2, "peak": l2_gbs, "unit": "GB/s",
                         "frac": achieved_l2 / l2_gbs if l2_gbs else None,
-                        "note": f"{WALK_BYTES_L2} B/step (5 gather sectors + 1 atomic sector); peak = L2-resident "
-                                "32 MiB device copy measured in this run"},
+                        "atomics_per_s": walk_rate, "atomic_peak_per_s": l2["atomics_per_s"],
+                        "note": f"walker: {WALK_SECTORS_L2} x 32 B sectors per step at L2 (one packed "
+                                "neighbourhood record + one hit atomic); peak = si_probe_l2_read over a 48 MiB "
+                                "L2-resident buffer measured in this run; atomic peak = si_probe_l2_atomics"},
         "clocks": clocks.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -347,22 +363,56 @@ def main():
         dist.destroy_process_group()
 
 
-def measure_l2_gbs(torch):
-    """L2-resident device copy bandwidth (read + write bytes), best of 20."""
-    a = torch.empty(16 << 20, dtype=torch.uint8, device="cuda")
-    b = torch.empty_like(a)
-    for _ in range(5):
-        b.copy_(a)
-    best = 0.0
-    for _ in range(20):
+def profile_jobs(args, wl):
+    """Untimed jobs on device-resident inputs, for profiler captures."""
+    import torch
+
+    from biomedisa_gb300 import interpolation as I
+
+    torch.cuda.set_device(0)
+    img, lab = make_inputs(args.workload)
+    data, labels = I.normalize_host_dtypes(img, lab)
+    img_t, lab_t = I.upload(data, labels)
+    for _ in range(args.profile_jobs):
+        t0 = time.perf_counter()
+        job, _ = run_job(img_t, I._IMG_DTYPES[data.dtype], lab_t, I._LAB_DTYPES[labels.dtype], wl)
+        torch.cuda.synchronize()
+        print(f"job: {job.total_steps()} walker steps, {time.perf_counter() - t0:.3f} s, "
+              f"walker={job.walker_used}, sweeps={getattr(job, 'rounds', None)}", flush=True)
+
+
+def measure_l2(torch):
+    """L2 ceilings measured here with the library's probe kernels: read
+    bandwidth over a 48 MiB L2-resident buffer (L1 bypassed, best of 10) and
+    random 4-byte atomic adds into a 16 MiB buffer (one 32-byte sector each)."""
+    from biomedisa_gb300 import _native as nat
+
+    stream = torch.cuda.current_stream().cuda_stream
+    buf = torch.zeros(48 << 20, dtype=torch.uint8, device="cuda")
+    sink = torch.zeros(1, dtype=torch.int32, device="cuda")
+    reps = 20
+    nat.call("si_probe_l2_read", buf.data_ptr(), buf.numel(), 2, sink.data_ptr(), stream)
+    best_read = 0.0
+    for _ in range(10):
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s.record()
-        for _ in range(50):
-            b.copy_(a)
+        nat.call("si_probe_l2_read", buf.data_ptr(), buf.numel(), reps, sink.data_ptr(), stream)
         e.record()
         torch.cuda.synchronize()
-        best = max(best, 50 * 2 * a.numel() / (s.elapsed_time(e) / 1e3) / 1e9)
-    return best
+        best_read = max(best_read, reps * buf.numel() / (s.elapsed_time(e) / 1e3) / 1e9)
+    words = 1 << 22
+    abuf = torch.zeros(words, dtype=torch.int32, device="cuda")
+    n = 1 << 30
+    nat.call("si_probe_l2_atomics", abuf.data_ptr(), words, 1 << 24, stream)
+    best_atom = 0.0
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        nat.call("si_probe_l2_atomics", abuf.data_ptr(), words, n, stream)
+        e.record()
+        torch.cuda.synchronize()
+        best_atom = max(best_atom, n / (s.elapsed_time(e) / 1e3))
+    return {"read_gbs": best_read, "atomics_per_s": best_atom}
 
 
 if __name__ == "__main__":

@@ -653,26 +653,28 @@ SortLayout sort_layout(const BrickGeom& g, uint64_t max_walks, int nol) {
 }  // namespace
 }  // namespace si
 
-extern "C" int si_walk_sorted_scratch(int Zc, int Yc, int Xc, uint64_t max_walks, int nol,
+extern "C" int si_walk_sorted_scratch(int Zc, int Yc, int Xc, uint64_t max_walks, int nol, int sort_edge,
                                       unsigned long long* bytes) {
   clear_error();
-  if (!bytes || Zc < 3 || Yc < 3 || Xc < 3 || nol < 1 || nol > 256)
+  if (!bytes || Zc < 3 || Yc < 3 || Xc < 3 || nol < 1 || nol > 256 || sort_edge < 0 || sort_edge > 1024)
     return set_error(SI_ERR_ARG, "si_walk_sorted_scratch: bad arguments");
-  *bytes = sort_layout(make_geom(Zc, Yc, Xc, kSortEdge), max_walks, nol).total;
+  *bytes = sort_layout(make_geom(Zc, Yc, Xc, sort_edge > 0 ? sort_edge : kSortEdge), max_walks, nol).total;
   return SI_OK;
 }
 
 extern "C" int si_walk_sorted(const void* packed, int work_is_float, int Zc, int Yc, int Xc,
                               const si_seed_t* seeds, const uint32_t* n_seeds, uint32_t max_seeds, int nbrw,
-                              int sorw, uint64_t key, uint32_t* hits, int nol, int sweep_steps, void* scratch,
-                              unsigned long long scratch_bytes, int* rounds_out, void* stream) {
+                              int sorw, uint64_t key, uint32_t* hits, int nol, int sweep_steps, int sort_edge,
+                              void* scratch, unsigned long long scratch_bytes, int* rounds_out, void* stream) {
   clear_error();
   if (!packed || !seeds || !n_seeds || !hits || !scratch) return set_error(SI_ERR_ARG, "si_walk_sorted: null pointer");
   if (Zc < 3 || Yc < 3 || Xc < 3 || nol < 1 || nol > 256) return set_error(SI_ERR_ARG, "si_walk_sorted: bad dims");
   if ((uint64_t)Zc * Yc * Xc > 0xFFFFFFFFull) return set_error(SI_ERR_LIMIT, "si_walk_sorted: volume above 2^32");
   if (nbrw < 0 || sorw < 0 || (uint64_t)nbrw * (uint64_t)sorw >= (1ull << 24))
     return set_error(SI_ERR_LIMIT, "si_walk_sorted: nbrw*sorw must be below 2^24");
-  if (sweep_steps <= 0) sweep_steps = 64;
+  if (sweep_steps <= 0) sweep_steps = 32;
+  if (sort_edge <= 0) sort_edge = kSortEdge;
+  if (sort_edge > 1024) return set_error(SI_ERR_ARG, "si_walk_sorted: sort_edge above 1024");
   cudaStream_t st = as_stream(stream);
   if (rounds_out) *rounds_out = 0;
   uint32_t ns = 0;
@@ -683,7 +685,8 @@ extern "C" int si_walk_sorted(const void* packed, int work_is_float, int Zc, int
   const uint64_t walks = (uint64_t)ns * (uint64_t)nbrw;
   if (walks == 0 || sorw == 0) return SI_OK;
   if (walks >= 0xFFFFFFFFull) return set_error(SI_ERR_LIMIT, "si_walk_sorted: more than 2^32 walks");
-  const BrickGeom g = make_geom(Zc, Yc, Xc, kSortEdge);
+  const BrickGeom g = make_geom(Zc, Yc, Xc, sort_edge);
+  if ((uint64_t)g.nb * (uint64_t)nol >= 0xFFFFFFFFull) return set_error(SI_ERR_LIMIT, "si_walk_sorted: too many buckets");
   const SortLayout L = sort_layout(g, walks, nol);
   if (scratch_bytes < L.total)
     return set_error(SI_ERR_ARG, "si_walk_sorted: scratch of %llu bytes, %llu needed", scratch_bytes,

@@ -145,56 +145,86 @@ __device__ __forceinline__ float ld(const void* p, size_t i) {
   return static_cast<const float*>(p)[i];
 }
 
+// 2.5-D tiled smoothing step: a 32x8 tile of threads marches
+// along z over a chunk of planes, keeping planes z-1, z, z+1 of the tile plus a
+// one-voxel halo in shared memory, so every value is read from global memory
+// about 1.3 times per iteration instead of being gathered 19 times.
+constexpr int kTX = 32, kTY = 8, kZChunk = 16;
+
 template <bool kSrcU32>
-__global__ void __launch_bounds__(256) smooth_step_kernel(const void* __restrict__ src, float* __restrict__ dst,
-                                                          int Zc, int Yc, int Xc) {
-  const size_t X = (size_t)Xc;
-  const size_t F = (size_t)Yc * Xc;
-  const size_t V = F * Zc;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < V; i += stride) {
-    const int xc = (int)(i % Xc);
-    const uint64_t zy = i / Xc;
-    const int yc = (int)(zy % Yc);
-    const int zc = (int)(zy / Yc);
-    const float c = ld<kSrcU32>(src, i);
-    if (!(zc > 0 && yc > 0 && xc > 0 && zc < Zc - 1 && yc < Yc - 1 && xc < Xc - 1)) {
-      dst[i] = c;
-      continue;
+__global__ void __launch_bounds__(kTX * kTY) smooth_tile_kernel(const void* __restrict__ src, float* __restrict__ dst,
+                                                               int Zc, int Yc, int Xc) {
+  __shared__ float pl[3][kTY + 2][kTX + 2];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
+  const int zb = blockIdx.z * kZChunk;
+  const int ze = min(zb + kZChunk, Zc);
+  const size_t X = (size_t)Xc, F = (size_t)Yc * Xc;
+  const int x = x0 + tx, y = y0 + ty;
+  const int tid = ty * kTX + tx;
+  // loads plane z (clamped to the volume; outside values are never used) into slot s
+  auto load_plane = [&](int z, int sidx) {
+    for (int i = tid; i < (kTY + 2) * (kTX + 2); i += kTX * kTY) {
+      const int ly = i / (kTX + 2), lx = i - ly * (kTX + 2);
+      const int gy = y0 + ly - 1, gx = x0 + lx - 1;
+      float v = 0.0f;
+      if (z >= 0 && z < Zc && gy >= 0 && gy < Yc && gx >= 0 && gx < Xc)
+        v = ld<kSrcU32>(src, (size_t)z * F + (size_t)gy * X + gx);
+      pl[sidx][ly][lx] = v;
     }
-    const float c2 = __fmul_rn(2.0f, c);
-    const float xm = ld<kSrcU32>(src, i - 1), xp = ld<kSrcU32>(src, i + 1);
-    const float ym = ld<kSrcU32>(src, i - X), yp = ld<kSrcU32>(src, i + X);
-    const float zm = ld<kSrcU32>(src, i - F), zp = ld<kSrcU32>(src, i + F);
-    const float dx = __fmul_rn(__fsub_rn(xm, xp), 0.5f);
-    const float dxx = __fadd_rn(__fsub_rn(xm, c2), xp);
-    const float dx2 = __fmul_rn(dx, dx);
-    const float dy = __fmul_rn(__fsub_rn(ym, yp), 0.5f);
-    const float dyy = __fadd_rn(__fsub_rn(ym, c2), yp);
-    const float dy2 = __fmul_rn(dy, dy);
-    const float dz = __fmul_rn(__fsub_rn(zm, zp), 0.5f);
-    const float dzz = __fadd_rn(__fsub_rn(zm, c2), zp);
-    const float dz2 = __fmul_rn(dz, dz);
-    const float dxy = __fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(ld<kSrcU32>(src, i - X - 1), ld<kSrcU32>(src, i + X + 1)),
-                                                    ld<kSrcU32>(src, i - X + 1)),
-                                          ld<kSrcU32>(src, i + X - 1)),
-                                0.25f);
-    const float dxz = __fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(ld<kSrcU32>(src, i + F - 1), ld<kSrcU32>(src, i - F + 1)),
-                                                    ld<kSrcU32>(src, i + F + 1)),
-                                          ld<kSrcU32>(src, i - F - 1)),
-                                0.25f);
-    const float dyz = __fmul_rn(__fsub_rn(__fsub_rn(__fadd_rn(ld<kSrcU32>(src, i + F - X), ld<kSrcU32>(src, i - F + X)),
-                                                    ld<kSrcU32>(src, i + F + X)),
-                                          ld<kSrcU32>(src, i - F - X)),
-                                0.25f);
-    float num = __fadd_rn(__fmul_rn(dxx, __fadd_rn(dy2, dz2)), __fmul_rn(dyy, __fadd_rn(dx2, dz2)));
-    num = __fadd_rn(num, __fmul_rn(dzz, __fadd_rn(dx2, dy2)));
-    num = __fsub_rn(num, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, dx), dy), dxy));
-    num = __fsub_rn(num, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, dx), dz), dxz));
-    num = __fsub_rn(num, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, dy), dz), dyz));
-    const float den = __fadd_rn(__fadd_rn(__fadd_rn(dx2, dy2), dz2), 1e-10f);
-    const float curv = __fdiv_rn(num, den);
-    dst[i] = __fadd_rn(c, __fmul_rn(0.01f, curv));
+  };
+  load_plane(zb - 1, 0);
+  load_plane(zb, 1);
+  int sm = 0, s0 = 1, sp = 2;
+  for (int z = zb; z < ze; ++z) {
+    load_plane(z + 1, sp);
+    __syncthreads();
+    if (x < Xc && y < Yc) {
+      const int lx = tx + 1, ly = ty + 1;
+      const float c = pl[s0][ly][lx];
+      const size_t i = (size_t)z * F + (size_t)y * X + x;
+      if (!(z > 0 && y > 0 && x > 0 && z < Zc - 1 && y < Yc - 1 && x < Xc - 1)) {
+        dst[i] = c;
+      } else {
+        const float c2 = __fmul_rn(2.0f, c);
+        const float xm = pl[s0][ly][lx - 1], xp = pl[s0][ly][lx + 1];
+        const float ym = pl[s0][ly - 1][lx], yp = pl[s0][ly + 1][lx];
+        const float zm = pl[sm][ly][lx], zp = pl[sp][ly][lx];
+        const float dx = __fmul_rn(__fsub_rn(xm, xp), 0.5f);
+        const float dxx = __fadd_rn(__fsub_rn(xm, c2), xp);
+        const float dx2 = __fmul_rn(dx, dx);
+        const float dy = __fmul_rn(__fsub_rn(ym, yp), 0.5f);
+        const float dyy = __fadd_rn(__fsub_rn(ym, c2), yp);
+        const float dy2 = __fmul_rn(dy, dy);
+        const float dz = __fmul_rn(__fsub_rn(zm, zp), 0.5f);
+        const float dzz = __fadd_rn(__fsub_rn(zm, c2), zp);
+        const float dz2 = __fmul_rn(dz, dz);
+        const float dxy = __fmul_rn(
+            __fsub_rn(__fsub_rn(__fadd_rn(pl[s0][ly - 1][lx - 1], pl[s0][ly + 1][lx + 1]), pl[s0][ly - 1][lx + 1]),
+                      pl[s0][ly + 1][lx - 1]),
+            0.25f);
+        const float dxz = __fmul_rn(
+            __fsub_rn(__fsub_rn(__fadd_rn(pl[sp][ly][lx - 1], pl[sm][ly][lx + 1]), pl[sp][ly][lx + 1]),
+                      pl[sm][ly][lx - 1]),
+            0.25f);
+        const float dyz = __fmul_rn(
+            __fsub_rn(__fsub_rn(__fadd_rn(pl[sp][ly - 1][lx], pl[sm][ly + 1][lx]), pl[sp][ly + 1][lx]),
+                      pl[sm][ly - 1][lx]),
+            0.25f);
+        float num = __fadd_rn(__fmul_rn(dxx, __fadd_rn(dy2, dz2)), __fmul_rn(dyy, __fadd_rn(dx2, dz2)));
+        num = __fadd_rn(num, __fmul_rn(dzz, __fadd_rn(dx2, dy2)));
+        num = __fsub_rn(num, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, dx), dy), dxy));
+        num = __fsub_rn(num, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, dx), dz), dxz));
+        num = __fsub_rn(num, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, dy), dz), dyz));
+        const float den = __fadd_rn(__fadd_rn(__fadd_rn(dx2, dy2), dz2), 1e-10f);
+        dst[i] = __fadd_rn(c, __fmul_rn(0.01f, __fdiv_rn(num, den)));
+      }
+    }
+    __syncthreads();
+    const int t = sm;
+    sm = s0;
+    s0 = sp;
+    sp = t;
   }
 }
 
@@ -255,6 +285,8 @@ extern "C" int si_smooth(uint32_t* maps, float* tmp0, float* tmp1, int nol, int 
   if (Zc < 1 || Yc < 1 || Xc < 1 || iters < 0) return set_error(SI_ERR_ARG, "si_smooth: bad arguments");
   const size_t V = (size_t)Zc * Yc * Xc;
   const int block = 256, grid = grid_for(V, block);
+  const dim3 tblock(kTX, kTY);
+  const dim3 tgrid((Xc + kTX - 1) / kTX, (Yc + kTY - 1) / kTY, (Zc + kZChunk - 1) / kZChunk);
   cudaStream_t st = as_stream(stream);
   for (int l = 0; l < nol; ++l) {
     uint32_t* m = maps + (size_t)l * V;
@@ -270,9 +302,9 @@ extern "C" int si_smooth(uint32_t* maps, float* tmp0, float* tmp1, int nol, int 
     for (int it = 1; it <= iters; ++it) {
       float* dst = (it == iters && it > 1) ? mf : bufs[it & 1];
       if (it == 1)
-        smooth_step_kernel<true><<<grid, block, 0, st>>>(src, dst, Zc, Yc, Xc);
+        smooth_tile_kernel<true><<<tgrid, tblock, 0, st>>>(src, dst, Zc, Yc, Xc);
       else
-        smooth_step_kernel<false><<<grid, block, 0, st>>>(src, dst, Zc, Yc, Xc);
+        smooth_tile_kernel<false><<<tgrid, tblock, 0, st>>>(src, dst, Zc, Yc, Xc);
       src = dst;
     }
     if (iters == 1) {

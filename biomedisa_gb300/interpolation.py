@@ -212,10 +212,11 @@ class DeviceJob:
     def __init__(self, img: torch.Tensor, img_code: int, lab: torch.Tensor, lab_code: int, *, nbrw=10, sorw=4000,
                  allaxis=False, smooth=0, uncertainty=False, denoise=False, only="all", ignore="none",
                  rng_seed=DEFAULT_RNG_SEED, walk_grid=0, walk_block=0, walk_order=0, walker="auto",
-                 sweep_steps=64):
+                 sweep_steps=0, sort_edge=0):
         if walker not in WALKERS:
             raise ValueError(f"walker must be one of {WALKERS}")
         self.sweep_steps = int(sweep_steps)
+        self.sort_edge = int(sort_edge)
         self.walker = walker
         if img.dim() != 3 or lab.dim() != 3 or tuple(img.shape) != tuple(lab.shape):
             raise ValueError("image and labels must be 3-D volumes of the same shape")
@@ -325,7 +326,7 @@ class DeviceJob:
         if self.walker_used == "sorted":
             self.rounds = walk_sorted(self.packed, self.work_is_float, cp.Zc, cp.Yc, cp.Xc, self.seeds,
                                       self.n_seeds, self.seed_capacity, self.nbrw, self.sorw, self.rng_seed,
-                                      self.hits, nol, self.sweep_steps)
+                                      self.hits, nol, self.sweep_steps, self.sort_edge)
             self.launches += 6 * self.rounds + 4
             return
         nat.call("si_walk", _ptr(self.packed), int(self.work_is_float), cp.Zc, cp.Yc, cp.Xc, _ptr(self.seeds),
@@ -401,15 +402,17 @@ def walk_bricks(work, Zc, Yc, Xc, seeds, n_seeds, max_seeds, nbrw, sorw, key, hi
 
 
 def walk_sorted(packed, is_float, Zc, Yc, Xc, seeds, n_seeds, max_seeds, nbrw, sorw, key, hits, nol,
-                sweep_steps=64) -> int:
+                sweep_steps=0, sort_edge=0) -> int:
     """Sorted-sweep walker (si_walk_sorted) with scratch from the caching
     allocator. Returns the number of sweeps."""
     need = ctypes.c_ulonglong(0)
-    nat.call("si_walk_sorted_scratch", Zc, Yc, Xc, int(max_seeds) * int(nbrw), nol, ctypes.byref(need))
+    nat.call("si_walk_sorted_scratch", Zc, Yc, Xc, int(max_seeds) * int(nbrw), nol, int(sort_edge),
+             ctypes.byref(need))
     scratch = torch.empty(max(int(need.value), 1), dtype=torch.uint8, device=packed.device)
     rounds = ctypes.c_int(0)
     nat.call("si_walk_sorted", _ptr(packed), int(is_float), Zc, Yc, Xc, _ptr(seeds), _ptr(n_seeds), int(max_seeds),
-             int(nbrw), int(sorw), int(key), _ptr(hits), nol, int(sweep_steps), _ptr(scratch), int(need.value),
+             int(nbrw), int(sorw), int(key), _ptr(hits), nol, int(sweep_steps), int(sort_edge), _ptr(scratch),
+             int(need.value),
              ctypes.byref(rounds), _stream())
     return int(rounds.value)
 
@@ -431,7 +434,7 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
                         platform=None, allaxis=False, ignore="none", only="all", smooth=0, compression=True,
                         return_hits=False, img_id=None, label_id=None, remote=False, queue=0, clean=None, fill=None,
                         slicer=False, *, rng_seed=DEFAULT_RNG_SEED, device=None, return_device=False,
-                        walk_grid=0, walk_block=0, walk_order=0, walker="auto", sweep_steps=64):
+                        walk_grid=0, walk_block=0, walk_order=0, walker="auto", sweep_steps=0, sort_edge=0):
     """Smart interpolation of sparsely pre-segmented slices on one GB300.
 
     Same parameters and result keys as the reference
@@ -440,7 +443,8 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
     None as the reference does. ``platform`` is accepted and ignored (one CUDA
     device). Extra keyword-only arguments: ``rng_seed`` (Philox key),
     ``device``, ``return_device`` (keep results as device tensors), ``walker``
-    ('auto' = 'sorted': sorted sweeps of ``sweep_steps`` steps; 'tiles':
+    ('auto' = 'sorted': sorted sweeps of ``sweep_steps`` steps over bricks of
+    ``sort_edge``^3 voxels (0 = library defaults); 'tiles':
     shared-memory brick walker, uint8 only; 'packed': one thread per walk) and
     the packed walker's launch shape (``walk_grid``, ``walk_block``,
     ``walk_order``). All walkers give identical hit maps.
@@ -462,7 +466,7 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
     job = DeviceJob(img, _IMG_DTYPES[np.dtype(data.dtype)], lab, _LAB_DTYPES[np.dtype(labelData.dtype)], nbrw=nbrw,
                     sorw=sorw, allaxis=allaxis, smooth=smooth, uncertainty=uncertainty, denoise=denoise, only=only,
                     ignore=ignore, rng_seed=rng_seed, walk_grid=walk_grid, walk_block=walk_block,
-                    walk_order=walk_order, walker=walker, sweep_steps=sweep_steps)
+                    walk_order=walk_order, walker=walker, sweep_steps=sweep_steps, sort_edge=sort_edge)
     msg = job.analyze()
     if msg:
         return _err(msg)

@@ -192,14 +192,15 @@ int si_walk_bricks(const void* work, int Zc, int Yc, int Xc,
                    void* stream);
 
 /* Scratch bytes si_walk_sorted needs (crop dims, max walks = seeds * nbrw,
- * labels). */
+ * labels, sort brick edge; sort_edge <= 0 selects the default 8). */
 int si_walk_sorted_scratch(int Zc, int Yc, int Xc, uint64_t max_walks, int nol,
-                           unsigned long long* bytes);
+                           int sort_edge, unsigned long long* bytes);
 
 /* Sorted-sweep walker: the same walk and the same uint32 hit maps as si_walk
  * over packed records (si_pack_neighbours), run as sweeps in which every live
- * walker advances min(sweep_steps, steps left) steps (default 64 when <= 0);
- * between sweeps the walkers are counting-sorted by (label slot, 8^3 brick),
+ * walker advances min(sweep_steps, steps left) steps (default 32 when <= 0);
+ * between sweeps the walkers are counting-sorted by (label slot, brick of
+ * sort_edge^3 voxels; default 8 when <= 0),
  * so concurrently running walkers share a compact, cache-resident part of
  * the volume and of the hit maps. scratch: si_walk_sorted_scratch bytes;
  * rounds_out (nullable) receives the number of sweeps. nbrw * sorw must be
@@ -207,9 +208,9 @@ int si_walk_sorted_scratch(int Zc, int Yc, int Xc, uint64_t max_walks, int nol,
 int si_walk_sorted(const void* packed, int work_is_float, int Zc, int Yc,
                    int Xc, const si_seed_t* seeds, const uint32_t* n_seeds,
                    uint32_t max_seeds, int nbrw, int sorw, uint64_t key,
-                   uint32_t* hits, int nol, int sweep_steps, void* scratch,
-                   unsigned long long scratch_bytes, int* rounds_out,
-                   void* stream);
+                   uint32_t* hits, int nol, int sweep_steps, int sort_edge,
+                   void* scratch, unsigned long long scratch_bytes,
+                   int* rounds_out, void* stream);
 
 /* Per-voxel argmax over nol maps ([nol][Zc][Yc][Xc], uint32 hits or float32
  * smoothed maps), first maximum wins (np.argmax, rw_small.py:200). The label
@@ -237,6 +238,16 @@ int si_remap_labels(uint8_t* out, int Zc, int Yc, int Xc, int cz0, int cy0,
  * Zc*Yc*Xc each. */
 int si_smooth(uint32_t* maps, float* tmp0, float* tmp1, int nol, int Zc,
               int Yc, int Xc, int iters, void* stream);
+
+/* Measurement probes (no counterpart in the reference; used by bench.py for
+ * the walker's roofline denominators). si_probe_l2_read reads `bytes` of buf
+ * `reps` times with L1-bypassing 16-byte loads (sink: one uint32, almost never
+ * written). si_probe_l2_atomics performs n_atomics 4-byte atomic adds at
+ * scattered positions of buf (`words` uint32, a power of two). */
+int si_probe_l2_read(const void* buf, uint64_t bytes, int reps, uint32_t* sink,
+                     void* stream);
+int si_probe_l2_atomics(uint32_t* buf, uint64_t words, uint64_t n_atomics,
+                        void* stream);
 
 #ifdef __cplusplus
 }
