@@ -319,10 +319,12 @@ def main():
     achieved_payload = walk_rate * WALK_BYTES_PAYLOAD_U8 / 1e9
     achieved_l2 = walk_rate * WALK_SECTORS_L2 * 32 / 1e9
     traffic = None
+    sweeps = max(getattr(job, "rounds", 0) or 0, 1)
     tp = ROOT / "profiles" / "walker_traffic.json"
     if tp.exists():
         tj = json.loads(tp.read_text())
-        traffic = tj.get("dram_bytes_per_step", 0) * steps_per_job if tj.get("workload") == args.workload else None
+        if tj.get("workload") == args.workload:
+            traffic = tj["dram_bytes_per_step"] * steps_per_job / sweeps  # DRAM bytes per sweep launch
 
     line = {
         "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": world, "steps": args.steps,
@@ -337,9 +339,11 @@ def main():
         "gpu_launches": launches // max(args.steps, 1),
         "roofline": {"bound": "hbm", "achieved": achieved_payload, "peak": hbm, "unit": "GB/s",
                      "frac": achieved_payload / hbm, "traffic": traffic,
-                     "note": f"walker kernel; algorithmic bytes = {WALK_BYTES_PAYLOAD_U8} B/step logical payload "
-                             f"(6 neighbour bytes + 4-byte hit) x {steps_per_job} steps / CUDA-event duration; "
-                             f"peak {peak_kind}"},
+                     "note": f"walker (sweep_kernel, {sweeps} launches per job); algorithmic bytes = "
+                             f"{WALK_BYTES_PAYLOAD_U8} B/step logical payload (6 neighbour bytes + 4-byte hit) x "
+                             f"steps / CUDA-event walk duration; peak {peak_kind} (MEASURED_PEAKS.json hbm_gbs); "
+                             "traffic = DRAM bytes per sweep launch from profiles/sweep_kernel_allaxis.md "
+                             "(10.88 B/step, scaled by steps per launch)"},
         "roofline_l2": {"bound": "l2", "achieved": achieved_l2, "peak": l2_gbs, "unit": "GB/s",
                         "frac": achieved_l2 / l2_gbs if l2_gbs else None,
                         "atomics_per_s": walk_rate, "atomic_peak_per_s": l2["atomics_per_s"],

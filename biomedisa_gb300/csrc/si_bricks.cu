@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(kAdvThreads, 4) brick_advance_kernel(
 // ---------------------------------------------------------------------------
 // Sorted sweep: every live walker advances exactly min(K, steps left) steps over
 // the packed records in global memory (uniform work per thread). Walkers are
-// counting-sorted by (label slot, 8^3 brick) between sweeps, so the threads
+// counting-sorted by (label slot, 6^3 brick) between sweeps, so the threads
 // resident at any moment work on a compact slab of the volume and its records
 // and hit counters stay in L2.
 // ---------------------------------------------------------------------------
@@ -624,7 +624,7 @@ extern "C" int si_walk_bricks(const void* work, int Zc, int Yc, int Xc, const si
 
 namespace si {
 namespace {
-constexpr int kSortEdge = 8;
+constexpr int kSortEdge = 6;
 
 struct SortLayout {
   size_t states0, states1, counts, offsets, sums, ctrs, total;

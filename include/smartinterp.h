@@ -192,7 +192,7 @@ int si_walk_bricks(const void* work, int Zc, int Yc, int Xc,
                    void* stream);
 
 /* Scratch bytes si_walk_sorted needs (crop dims, max walks = seeds * nbrw,
- * labels, sort brick edge; sort_edge <= 0 selects the default 8). */
+ * labels, sort brick edge; sort_edge <= 0 selects the default 6). */
 int si_walk_sorted_scratch(int Zc, int Yc, int Xc, uint64_t max_walks, int nol,
                            int sort_edge, unsigned long long* bytes);
 
@@ -200,7 +200,7 @@ int si_walk_sorted_scratch(int Zc, int Yc, int Xc, uint64_t max_walks, int nol,
  * over packed records (si_pack_neighbours), run as sweeps in which every live
  * walker advances min(sweep_steps, steps left) steps (default 32 when <= 0);
  * between sweeps the walkers are counting-sorted by (label slot, brick of
- * sort_edge^3 voxels; default 8 when <= 0),
+ * sort_edge^3 voxels; default 6 when <= 0),
  * so concurrently running walkers share a compact, cache-resident part of
  * the volume and of the hit maps. scratch: si_walk_sorted_scratch bytes;
  * rounds_out (nullable) receives the number of sweeps. nbrw * sorw must be
