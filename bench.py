@@ -37,12 +37,32 @@ WORKLOADS = {
                          "slice, nbrw=10, sorw=4000, smooth=100", nbrw=10, sorw=4000, smooth=100, allaxis=True),
     "plain": dict(desc="plain uint8 128^3, 2 ellipsoids, labels every 10th z-slice, nbrw=10, sorw=4000, smooth=0",
                   nbrw=10, sorw=4000, smooth=0, allaxis=False),
+    "batch": dict(desc="batch of 32 uint16 volumes, sizes uniform in 64^3..(256,320,384) (z,y,x), 2-12 phases, "
+                       "labels every 4..20th z-slice, nbrw=10, sorw=4000, smooth=50; one batched walk, smoothing "
+                       "replayed from a CUDA graph, autotuned sweep parameters", nbrw=10, sorw=4000, smooth=50,
+                  allaxis=False),
     "large": dict(desc="large uint8 1024^3, 6 phases, labels every 12th z-slice, nbrw=10, sorw=4000, smooth=100",
                   nbrw=10, sorw=4000, smooth=100, allaxis=False),
 }
 
 WALK_SECTORS_L2 = 2  # per walker step at L2: one packed-record sector + one atomic sector
 WALK_BYTES_PAYLOAD_U8 = 10  # 6 neighbour bytes + one 4-byte hit per step
+
+
+def make_batch_inputs(seed: int = 0, count: int = 32):
+    from biomedisa_gb300 import synthetic as S
+
+    cache = Path(os.environ.get("SI_BENCH_CACHE", "/tmp")) / f"si_bench_batch_{seed}_{count}.npz"
+    if cache.exists():
+        z = np.load(cache)
+        return [z[f"img{i}"] for i in range(count)], [z[f"lab{i}"] for i in range(count)]
+    vols = S.batch_volumes(seed=seed, count=count)
+    imgs, labs = [v[0] for v in vols], [v[1] for v in vols]
+    try:
+        np.savez(cache, **{f"img{i}": a for i, a in enumerate(imgs)}, **{f"lab{i}": a for i, a in enumerate(labs)})
+    except OSError:
+        pass
+    return imgs, labs
 
 
 def make_inputs(name: str, seed: int = 0):
@@ -246,6 +266,9 @@ def main():
     if args.profile_jobs:
         profile_jobs(args, wl)
         return
+    if args.workload == "batch":
+        run_batch_bench(args, wl)
+        return
     if args.impl == "reference":
         run_reference(args, wl)
         return
@@ -365,6 +388,71 @@ def main():
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def run_batch_bench(args, wl):
+    """Batched workload: value = walker steps of all volumes / batch time on
+    device-resident volumes; e2e through smart_interpolation_batch."""
+    import torch
+
+    from biomedisa_gb300 import interpolation as I
+    from biomedisa_gb300 import smart_interpolation_batch
+    from biomedisa_gb300.batch import run_device_batch
+
+    world, rank, local = dist_setup()
+    imgs, labs = make_batch_inputs()
+    dev = []
+    for img, lab in zip(imgs, labs):
+        d, l = I.normalize_host_dtypes(img, lab)
+        ti, tl = I.upload(d, l)
+        dev.append((ti, I._IMG_DTYPES[d.dtype], tl, I._LAB_DTYPES[l.dtype]))
+    torch.cuda.synchronize()
+    l2buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    kw = dict(nbrw=wl["nbrw"], sorw=wl["sorw"], smooth=wl["smooth"])
+    for _ in range(args.warmup):
+        run_device_batch(dev, **kw)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    times, steps, rep = [], 0, {}
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush_l2(l2buf)
+            torch.cuda.synchronize()
+            barrier(world)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            jobs, res, rep = run_device_batch(dev, **kw)
+            e.record(stream)
+            torch.cuda.synchronize()
+            barrier(world)
+            times.append(s.elapsed_time(e))
+            steps = rep["walker_steps"]
+    ms = max_over_ranks(world, sum(times) / len(times))
+    value = world * steps / (ms / 1e3)
+    t_e2e = []
+    for _ in range(args.e2e_steps or args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = smart_interpolation_batch(imgs, labs, **kw)
+        torch.cuda.synchronize()
+        t_e2e.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(world, sum(t_e2e) / len(t_e2e))
+    line = {
+        "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded generator, no public dataset)",
+        "config": {"workload": wl["desc"], "global_batch": len(imgs), "parallelism": "single GPU",
+                   "l2": "256 MiB buffer written before every timed step"},
+        "voxels_per_s": world * sum(int(np.prod(a.shape)) for a in imgs) / (ms / 1e3),
+        "total_walker_steps": steps, "sweeps": rep.get("sweeps"), "sort_edge": rep.get("sort_edge"),
+        "sweep_steps": rep.get("sweep_steps"),
+        "e2e": {"value": world * steps / e2e_s, "unit": "walker-steps/s", "seconds": e2e_s,
+                "h2d_bytes_per_step": int(sum(a.nbytes for a in imgs) + sum(a.nbytes for a in labs)),
+                "d2h_bytes_per_step": int(sum(v.nbytes for r in out if r for v in r.values()))},
+        "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
 
 
 def profile_jobs(args, wl):

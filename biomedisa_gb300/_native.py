@@ -41,6 +41,9 @@ _SIGNATURES = {
     "si_walk_sorted_scratch": [_c_int, _c_int, _c_int, _c_u64, _c_int, _c_int, _c_void_p],
     "si_walk_sorted": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_void_p, _c_u32, _c_int, _c_int,
                        _c_u64, _c_void_p, _c_int, _c_int, _c_int, _c_void_p, _c_u64, _c_void_p, _c_void_p],
+    "si_walk_sorted_batch_scratch": [_c_void_p, _c_int, _c_int, _c_int, _c_void_p],
+    "si_walk_sorted_batch": [_c_void_p, _c_int, _c_int, _c_int, _c_u64, _c_int, _c_int, _c_void_p, _c_u64, _c_void_p,
+                             _c_void_p],
     "si_argmax": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int,
                   _c_void_p, _c_void_p, _c_void_p, _c_void_p],
     "si_remap_labels": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p,

@@ -20,6 +20,7 @@
 
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "si_common.cuh"
 #include "si_internal.h"
@@ -746,4 +747,295 @@ extern "C" int si_walk_sorted(const void* packed, int work_is_float, int Zc, int
   }
   if (rounds_out) *rounds_out = rounds;
   return check_launch("si_walk_sorted");
+}
+
+// ===========================================================================
+// Batched sorted sweeps: many volumes (uneven sizes, any label counts, uint8
+// or float32 records) walked together. A walker state carries its volume in
+// the top 8 bits of the step counter (t < 2^24), buckets are
+// (volume, label slot, brick) ranges of one global bucket space, and every
+// sweep launch advances the walkers of all volumes. Hit maps, randomness and
+// results per volume are exactly those of si_walk_sorted on that volume alone.
+// ===========================================================================
+namespace si {
+namespace {
+
+struct VolDesc {
+  const void* packed;
+  uint32_t* hits;
+  const SeedRec* seeds;
+  uint32_t F;       // Yc * Xc
+  int Zc, Yc, Xc;
+  int nby, nbx;     // bricks per row / column
+  uint32_t nb;      // bricks per label
+  uint32_t bucket0; // first bucket of this volume
+  uint64_t walk0;   // first global walk index of this volume (round 0)
+  uint32_t ns;      // seeds
+  int is_float;
+};
+
+__device__ __forceinline__ uint32_t bvol(const uint4& s) { return s.z >> 24; }
+__device__ __forceinline__ uint32_t bstep(const uint4& s) { return s.z & 0xFFFFFFu; }
+__device__ __forceinline__ bool blive(const uint4& s) { return bstep(s) != (s.w & 0xFFFFFFu); }
+
+__device__ __forceinline__ uint32_t bbucket(const VolDesc& v, int edge, const uint4& s) {
+  const uint32_t z = s.x / v.F;
+  const uint32_t r = s.x - z * v.F;
+  const uint32_t y = r / (uint32_t)v.Xc;
+  const uint32_t x = r - y * (uint32_t)v.Xc;
+  const uint32_t e = (uint32_t)edge;
+  const uint32_t brick = (z / e * (uint32_t)v.nby + y / e) * (uint32_t)v.nbx + x / e;
+  return v.bucket0 + (s.w >> 24) * v.nb + brick;
+}
+
+template <bool kFirst>
+__device__ __forceinline__ bool bfetch(uint64_t i, uint64_t n, const uint4* __restrict__ states,
+                                       const VolDesc* __restrict__ vols, int n_vols, int sorw, uint4& s) {
+  if (i >= n) return false;
+  if (kFirst) {
+    // volume holding global walk i (volumes are few: linear search)
+    int v = 0;
+    while (v + 1 < n_vols && vols[v + 1].walk0 <= i) ++v;
+    const VolDesc& d = vols[v];
+    const uint64_t j = i - d.walk0;
+    const uint32_t w = (uint32_t)(j / d.ns);
+    const uint32_t sidx = (uint32_t)(j - (uint64_t)w * d.ns);
+    const SeedRec sd = d.seeds[sidx];
+    s = make_uint4(sd.pos, sidx, (w * (uint32_t)sorw) | ((uint32_t)v << 24),
+                   ((w + 1u) * (uint32_t)sorw) | (seed_slot(sd.meta) << 24));
+    return true;
+  }
+  s = states[i];
+  return blive(s);
+}
+
+template <bool kFirst, bool kScatter>
+__global__ void __launch_bounds__(256) bbucket_kernel(const uint4* __restrict__ states_in, uint64_t n,
+                                                      const VolDesc* __restrict__ vols, int n_vols, int sorw,
+                                                      int edge, uint32_t* __restrict__ counts,
+                                                      const uint32_t* __restrict__ offsets,
+                                                      uint4* __restrict__ states_out) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+    uint4 s;
+    const bool ok = bfetch<kFirst>(base + lane, n, states_in, vols, n_vols, sorw, s);
+    const uint32_t key = ok ? bbucket(vols[bvol(s)], edge, s) : 0u;
+    const uint32_t act = __ballot_sync(0xffffffffu, ok);
+    if (ok) {
+      const uint32_t peers = __match_any_sync(act, key);
+      const int leader = __ffs(peers) - 1;
+      const uint32_t cnt = __popc(peers);
+      if (!kScatter) {
+        if (lane == leader) atomicAdd(&counts[key], cnt);
+      } else {
+        uint32_t b = 0;
+        if (lane == leader) b = atomicAdd(&counts[key], cnt);
+        b = __shfl_sync(peers, b, leader);
+        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        states_out[offsets[key] + b + rank] = s;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) bsweep_kernel(const VolDesc* __restrict__ vols, int n_vols,
+                                                     uint4* __restrict__ states, uint32_t n_live, uint32_t K,
+                                                     uint32_t k0, uint32_t k1) {
+  __shared__ int32_t s_delta[256 * 6];  // move offsets of every volume
+  for (int i = threadIdx.x; i < n_vols * 6; i += blockDim.x) {
+    const VolDesc& d = vols[i / 6];
+    const int dir = i % 6;
+    const int32_t mag = dir < 2 ? (int32_t)d.F : (dir < 4 ? d.Xc : 1);
+    s_delta[i] = (dir & 1) ? -mag : mag;
+  }
+  __syncthreads();
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_live; i += stride) {
+    uint4 st = states[i];
+    const uint32_t v = bvol(st);
+    const VolDesc& d = vols[v];
+    const SeedRec sd = d.seeds[st.y];
+    const uint32_t t = bstep(st);
+    const uint32_t te = st.w & 0xFFFFFFu;
+    const uint32_t t_end = min(t + K, te);
+    uint32_t* __restrict__ hl = d.hits + (size_t)(st.w >> 24) * ((size_t)d.F * d.Zc);
+    if (d.is_float)
+      st.x = walk_steps<true>(d.packed, st.x, t, t_end, sd.c, sd.b, sd.pos, seed_axis(sd.meta), seed_label(sd.meta),
+                              k0, k1, hl, s_delta + 6 * v);
+    else
+      st.x = walk_steps<false>(d.packed, st.x, t, t_end, sd.c, sd.b, sd.pos, seed_axis(sd.meta),
+                               seed_label(sd.meta), k0, k1, hl, s_delta + 6 * v);
+    st.z = t_end | (st.z & 0xFF000000u);
+    states[i] = st;
+  }
+}
+
+}  // namespace
+}  // namespace si
+
+namespace {
+// host helper: descriptors, bucket totals, scratch layout
+struct BatchPlan {
+  std::vector<si::VolDesc> vols;
+  uint64_t walks = 0;
+  uint32_t nbt = 0;
+  size_t off_vols = 0, off_states0 = 0, off_states1 = 0, off_counts = 0, off_offsets = 0, off_sums = 0,
+         off_ctrs = 0, total = 0;
+};
+
+int make_batch_plan(const si_volume_t* vols, int n_vols, int nbrw, int edge, const uint32_t* ns_host,
+                    BatchPlan& P) {
+  P.vols.resize(n_vols);
+  uint64_t bucket = 0, walk = 0;
+  for (int v = 0; v < n_vols; ++v) {
+    const si_volume_t& in = vols[v];
+    if (!in.packed || !in.hits || !in.seeds || !in.n_seeds || in.Zc < 3 || in.Yc < 3 || in.Xc < 3 || in.nol < 1 ||
+        in.nol > 256)
+      return si::set_error(SI_ERR_ARG, "si_walk_sorted_batch: bad volume %d", v);
+    if ((uint64_t)in.Zc * in.Yc * in.Xc > 0xFFFFFFFFull)
+      return si::set_error(SI_ERR_LIMIT, "si_walk_sorted_batch: volume %d above 2^32 voxels", v);
+    si::VolDesc& d = P.vols[v];
+    d.packed = in.packed;
+    d.hits = in.hits;
+    d.seeds = reinterpret_cast<const si::SeedRec*>(in.seeds);
+    d.Zc = in.Zc;
+    d.Yc = in.Yc;
+    d.Xc = in.Xc;
+    d.F = (uint32_t)in.Yc * (uint32_t)in.Xc;
+    const int nbz = (in.Zc + edge - 1) / edge;
+    d.nby = (in.Yc + edge - 1) / edge;
+    d.nbx = (in.Xc + edge - 1) / edge;
+    d.nb = (uint32_t)nbz * d.nby * d.nbx;
+    d.bucket0 = (uint32_t)bucket;
+    d.walk0 = walk;
+    d.ns = ns_host ? (ns_host[v] < in.max_seeds ? ns_host[v] : in.max_seeds) : in.max_seeds;
+    d.is_float = in.work_is_float;
+    bucket += (uint64_t)d.nb * in.nol;
+    walk += (uint64_t)d.ns * (uint64_t)nbrw;
+  }
+  if (bucket >= 0xFFFFFFFFull) return si::set_error(SI_ERR_LIMIT, "si_walk_sorted_batch: too many buckets");
+  if (walk >= 0xFFFFFFFFull) return si::set_error(SI_ERR_LIMIT, "si_walk_sorted_batch: more than 2^32 walks");
+  P.walks = walk;
+  P.nbt = (uint32_t)bucket;
+  const uint64_t nblocks = (P.nbt + si::kScanBlock - 1) / si::kScanBlock;
+  size_t off = 0;
+  P.off_vols = off;
+  off = si::align_up(off + n_vols * sizeof(si::VolDesc), 256);
+  P.off_states0 = off;
+  off = si::align_up(off + P.walks * sizeof(uint4), 256);
+  P.off_states1 = off;
+  off = si::align_up(off + P.walks * sizeof(uint4), 256);
+  P.off_counts = off;
+  off = si::align_up(off + ((size_t)P.nbt + 1) * sizeof(uint32_t), 256);
+  P.off_offsets = off;
+  off = si::align_up(off + ((size_t)P.nbt + 1) * sizeof(uint32_t), 256);
+  P.off_sums = off;
+  off = si::align_up(off + (nblocks + 1) * sizeof(uint32_t), 256);
+  P.off_ctrs = off;
+  off = si::align_up(off + 4 * sizeof(uint32_t), 256);
+  P.total = off;
+  return SI_OK;
+}
+}  // namespace
+
+extern "C" int si_walk_sorted_batch_scratch(const si_volume_t* vols, int n_vols, int nbrw, int sort_edge,
+                                            unsigned long long* bytes) {
+  clear_error();
+  if (!vols || !bytes || n_vols < 1 || n_vols > 256 || nbrw < 0 || sort_edge < 0 || sort_edge > 1024)
+    return set_error(SI_ERR_ARG, "si_walk_sorted_batch_scratch: bad arguments");
+  BatchPlan P;
+  const int rc = make_batch_plan(vols, n_vols, nbrw, sort_edge > 0 ? sort_edge : kSortEdge, nullptr, P);
+  if (rc) return rc;
+  *bytes = P.total;
+  return SI_OK;
+}
+
+extern "C" int si_walk_sorted_batch(const si_volume_t* vols, int n_vols, int nbrw, int sorw, uint64_t key,
+                                    int sweep_steps, int sort_edge, void* scratch, unsigned long long scratch_bytes,
+                                    int* rounds_out, void* stream) {
+  clear_error();
+  if (!vols || !scratch || n_vols < 1 || n_vols > 256) return set_error(SI_ERR_ARG, "si_walk_sorted_batch: bad args");
+  if (nbrw < 0 || sorw < 0 || (uint64_t)nbrw * (uint64_t)sorw >= (1ull << 24))
+    return set_error(SI_ERR_LIMIT, "si_walk_sorted_batch: nbrw*sorw must be below 2^24");
+  if (sweep_steps <= 0) sweep_steps = 32;
+  if (sort_edge <= 0) sort_edge = kSortEdge;
+  if (sort_edge > 1024) return set_error(SI_ERR_ARG, "si_walk_sorted_batch: sort_edge above 1024");
+  cudaStream_t st = as_stream(stream);
+  if (rounds_out) *rounds_out = 0;
+  std::vector<uint32_t> ns(n_vols, 0);
+  for (int v = 0; v < n_vols; ++v) {
+    if (!vols[v].n_seeds) return set_error(SI_ERR_ARG, "si_walk_sorted_batch: volume %d has no seed count", v);
+    if (cudaMemcpyAsync(&ns[v], vols[v].n_seeds, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_walk_sorted_batch: reading seed counts failed");
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess)
+    return set_error(SI_ERR_CUDA, "si_walk_sorted_batch: reading seed counts failed");
+  BatchPlan P;
+  int rc = make_batch_plan(vols, n_vols, nbrw, sort_edge, ns.data(), P);
+  if (rc) return rc;
+  if (P.walks == 0 || sorw == 0) return SI_OK;
+  BatchPlan Pmax;  // scratch is sized for max_seeds
+  rc = make_batch_plan(vols, n_vols, nbrw, sort_edge, nullptr, Pmax);
+  if (rc) return rc;
+  if (scratch_bytes < Pmax.total)
+    return set_error(SI_ERR_ARG, "si_walk_sorted_batch: scratch of %llu bytes, %llu needed", scratch_bytes,
+                     (unsigned long long)Pmax.total);
+  uint8_t* base = static_cast<uint8_t*>(scratch);
+  // layout of the max-seed plan; the actual walks fit in it
+  VolDesc* d_vols = reinterpret_cast<VolDesc*>(base + Pmax.off_vols);
+  uint4* states[2] = {reinterpret_cast<uint4*>(base + Pmax.off_states0),
+                      reinterpret_cast<uint4*>(base + Pmax.off_states1)};
+  uint32_t* counts = reinterpret_cast<uint32_t*>(base + Pmax.off_counts);
+  uint32_t* offsets = reinterpret_cast<uint32_t*>(base + Pmax.off_offsets);
+  uint32_t* sums = reinterpret_cast<uint32_t*>(base + Pmax.off_sums);
+  uint32_t* ctrs = reinterpret_cast<uint32_t*>(base + Pmax.off_ctrs);
+  if (cudaMemcpyAsync(d_vols, P.vols.data(), n_vols * sizeof(VolDesc), cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return set_error(SI_ERR_CUDA, "si_walk_sorted_batch: descriptor upload failed");
+  const uint32_t nbt = P.nbt;
+  const uint32_t nblocks = (nbt + kScanBlock - 1) / kScanBlock;
+  const int sms = sm_count();
+  const int gb = sms * 8;
+  const uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
+  int cur = 0, rounds = 0;
+  uint64_t n_prev = P.walks;
+  for (;; ++rounds) {
+    const bool first = rounds == 0;
+    if (cudaMemsetAsync(counts, 0, (size_t)(nbt + 1) * sizeof(uint32_t), st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_walk_sorted_batch: memset failed");
+    if (first)
+      bbucket_kernel<true, false><<<gb, 256, 0, st>>>(nullptr, n_prev, d_vols, n_vols, sorw, sort_edge, counts,
+                                                      nullptr, nullptr);
+    else
+      bbucket_kernel<false, false><<<gb, 256, 0, st>>>(states[cur], n_prev, d_vols, n_vols, sorw, sort_edge, counts,
+                                                       nullptr, nullptr);
+    scan_sums_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums);
+    scan_top_kernel<<<1, 1024, 0, st>>>(sums, nblocks);
+    scan_apply_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums, offsets, ctrs);
+    uint32_t live_now = 0;
+    if (cudaMemcpyAsync(&live_now, ctrs, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_walk_sorted_batch: round %d: %s", rounds,
+                       cudaGetErrorString(cudaGetLastError()));
+    if (live_now == 0) break;
+    if (cudaMemsetAsync(counts, 0, (size_t)(nbt + 1) * sizeof(uint32_t), st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_walk_sorted_batch: memset failed");
+    const int nxt = first ? 0 : 1 - cur;
+    if (first)
+      bbucket_kernel<true, true><<<gb, 256, 0, st>>>(nullptr, n_prev, d_vols, n_vols, sorw, sort_edge, counts, offsets,
+                                                     states[nxt]);
+    else
+      bbucket_kernel<false, true><<<gb, 256, 0, st>>>(states[cur], n_prev, d_vols, n_vols, sorw, sort_edge, counts,
+                                                      offsets, states[nxt]);
+    cur = nxt;
+    const uint64_t want_blocks = ((uint64_t)live_now + 255) / 256;
+    const uint32_t blocks = (uint32_t)(want_blocks < (uint64_t)sms * 8 ? want_blocks : (uint64_t)sms * 8);
+    bsweep_kernel<<<blocks, 256, 0, st>>>(d_vols, n_vols, states[cur], live_now, (uint32_t)sweep_steps, k0, k1);
+    rc = check_launch("si_walk_sorted_batch: sweep");
+    if (rc) return rc;
+    n_prev = live_now;
+    if (rounds > (1 << 24)) return set_error(SI_ERR_LIMIT, "si_walk_sorted_batch: no convergence");
+  }
+  if (rounds_out) *rounds_out = rounds;
+  return check_launch("si_walk_sorted_batch");
 }

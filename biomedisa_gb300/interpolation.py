@@ -355,9 +355,8 @@ class DeviceJob:
         full[:, cp.cz0:cp.cz0 + cp.Zc, cp.cy0:cp.cy0 + cp.Yc, cp.cx0:cp.cx0 + cp.Xc] = self.hits.float()
         return full[:, 1:-1, 1:-1, 1:-1]
 
-    def post(self, return_hits=False):
-        """argmax (+uncertainty), optional hits, optional smoothing. Returns a
-        dict of device tensors."""
+    def post_regular(self, return_hits=False):
+        """argmax (+ uncertainty) and optional hit maps; a dict of device tensors."""
         res = {}
         out, uq = self._labels_from(self.hits, False, self.uncertainty)
         res["regular"] = out
@@ -365,15 +364,30 @@ class DeviceJob:
             res["uncertainty"] = uq
         if return_hits:
             res["hits"] = self.hits_full().contiguous()
+        return res
+
+    def smooth_launch(self, tmp0: torch.Tensor, tmp1: torch.Tensor):
+        """Launches the smoothing iterations (in place on the hit maps); only
+        kernel launches on the current stream, so it can be graph-captured."""
+        cp = self.cplan
+        nat.call("si_smooth", _ptr(self.hits), _ptr(tmp0), _ptr(tmp1), self.lplan.nol, cp.Zc, cp.Yc, cp.Xc,
+                 self.smooth, _stream())
+        self.launches += self.lplan.nol * max(self.smooth, 1)
+
+    def post_smooth(self):
+        sm, _ = self._labels_from(self.hits, True, False)
+        return sm
+
+    def post(self, return_hits=False):
+        """argmax (+uncertainty), optional hits, optional smoothing. Returns a
+        dict of device tensors."""
+        res = self.post_regular(return_hits)
         if self.smooth:
             cp = self.cplan
             tmp0 = torch.empty(cp.voxels, dtype=torch.float32, device=self.dev)
             tmp1 = torch.empty(cp.voxels, dtype=torch.float32, device=self.dev)
-            nat.call("si_smooth", _ptr(self.hits), _ptr(tmp0), _ptr(tmp1), self.lplan.nol, cp.Zc, cp.Yc, cp.Xc,
-                     self.smooth, _stream())
-            self.launches += self.lplan.nol * max(self.smooth, 1)
-            sm, _ = self._labels_from(self.hits, True, False)
-            res["smooth"] = sm
+            self.smooth_launch(tmp0, tmp1)
+            res["smooth"] = self.post_smooth()
         return res
 
     def total_steps(self) -> int:

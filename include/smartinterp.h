@@ -53,6 +53,20 @@ typedef struct {
   uint32_t meta;
 } si_seed_t;
 
+/* One volume of a batched walk (si_walk_sorted_batch). packed: its packed
+ * records (si_pack_neighbours); hits: uint32 [nol][Zc][Yc][Xc], caller-zeroed;
+ * seeds / n_seeds / max_seeds: as for si_walk. */
+typedef struct {
+  const void* packed;
+  uint32_t* hits;
+  const si_seed_t* seeds;
+  const uint32_t* n_seeds;
+  uint32_t max_seeds;
+  int Zc, Yc, Xc;
+  int nol;
+  int work_is_float;
+} si_volume_t;
+
 /* Library version (major*10000 + minor*100 + patch). */
 int si_version(void);
 
@@ -211,6 +225,24 @@ int si_walk_sorted(const void* packed, int work_is_float, int Zc, int Yc,
                    uint32_t* hits, int nol, int sweep_steps, int sort_edge,
                    void* scratch, unsigned long long scratch_bytes,
                    int* rounds_out, void* stream);
+
+/* Scratch bytes si_walk_sorted_batch needs for these volumes (host array of
+ * n_vols descriptors, at most 256). */
+int si_walk_sorted_batch_scratch(const si_volume_t* vols, int n_vols,
+                                 int nbrw, int sort_edge,
+                                 unsigned long long* bytes);
+
+/* Batched sorted sweeps: the walks of all n_vols volumes (uneven sizes,
+ * uint8 or float records, any label counts) advance together in every sweep
+ * launch, bucketed by (volume, label slot, brick). Each volume's hit maps
+ * equal si_walk_sorted / si_walk on that volume alone (same key). vols is a
+ * HOST array; scratch: si_walk_sorted_batch_scratch bytes. Replaces running
+ * the reference once per volume. */
+int si_walk_sorted_batch(const si_volume_t* vols, int n_vols, int nbrw,
+                         int sorw, uint64_t key, int sweep_steps,
+                         int sort_edge, void* scratch,
+                         unsigned long long scratch_bytes, int* rounds_out,
+                         void* stream);
 
 /* Per-voxel argmax over nol maps ([nol][Zc][Yc][Xc], uint32 hits or float32
  * smoothed maps), first maximum wins (np.argmax, rw_small.py:200). The label
