@@ -467,10 +467,14 @@ def profile_jobs(args, wl):
     img_t, lab_t = I.upload(data, labels)
     for _ in range(args.profile_jobs):
         t0 = time.perf_counter()
-        job, _ = run_job(img_t, I._IMG_DTYPES[data.dtype], lab_t, I._LAB_DTYPES[labels.dtype], wl)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        job, _ = run_job(img_t, I._IMG_DTYPES[data.dtype], lab_t, I._LAB_DTYPES[labels.dtype], wl, events=ev)
         torch.cuda.synchronize()
-        print(f"job: {job.total_steps()} walker steps, {time.perf_counter() - t0:.3f} s, "
-              f"walker={job.walker_used}, sweeps={getattr(job, 'rounds', None)}", flush=True)
+        walk_s = ev[0].elapsed_time(ev[1]) / 1e3
+        print(f"job: {job.total_steps()} walker steps, {time.perf_counter() - t0:.3f} s, walk {walk_s:.3f} s "
+              f"({job.total_steps() / walk_s:.3e} steps/s), walker={job.walker_used}, "
+              f"sweeps={getattr(job, 'rounds', None)}, crop={job.cplan.crop}, seeds={int(job.n_seeds.item())}",
+              flush=True)
 
 
 def measure_l2(torch):

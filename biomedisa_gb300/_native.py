@@ -50,6 +50,20 @@ _SIGNATURES = {
                         _c_void_p, _c_int, _c_void_p],
     "si_probe_l2_read": [_c_void_p, _c_u64, _c_int, _c_void_p, _c_void_p],
     "si_probe_l2_atomics": [_c_void_p, _c_u64, _c_u64, _c_void_p],
+    "si_nn_conv3d_fwd": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int,
+                         _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_nn_conv3d_wgrad": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int,
+                           _c_int, _c_int, _c_void_p],
+    "si_nn_flip_weights": [_c_void_p, _c_void_p, _c_int, _c_int, _c_void_p],
+    "si_nn_relu_bwd": [_c_void_p, _c_void_p, _c_void_p, ctypes.c_int64, _c_void_p],
+    "si_nn_xent": [_c_void_p, _c_void_p, _c_void_p, ctypes.c_int64, _c_int, _c_int, _c_float, _c_void_p, _c_void_p,
+                   _c_void_p],
+    "si_nn_adamw": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, ctypes.c_int64, _c_float, _c_float,
+                    _c_float, _c_float, _c_float, _c_int, _c_void_p],
+    "si_nn_features": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int,
+                       _c_int, _c_int, _c_void_p, _c_void_p],
+    "si_nn_probs": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_int, _c_int, _c_void_p],
+    "si_smooth_f32": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
     "si_smooth": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
 }
 

@@ -314,3 +314,28 @@ extern "C" int si_smooth(uint32_t* maps, float* tmp0, float* tmp1, int nol, int 
   }
   return check_launch("si_smooth");
 }
+
+extern "C" int si_smooth_f32(float* maps, float* tmp0, float* tmp1, int nol, int Zc, int Yc, int Xc, int iters,
+                             void* stream) {
+  clear_error();
+  if (!maps || !tmp0 || !tmp1) return set_error(SI_ERR_ARG, "si_smooth_f32: null pointer");
+  if (nol < 1 || nol > 256) return set_error(SI_ERR_ARG, "si_smooth_f32: nol must be 1..256");
+  if (Zc < 1 || Yc < 1 || Xc < 1 || iters < 0) return set_error(SI_ERR_ARG, "si_smooth_f32: bad arguments");
+  const size_t V = (size_t)Zc * Yc * Xc;
+  const dim3 tblock(kTX, kTY);
+  const dim3 tgrid((Xc + kTX - 1) / kTX, (Yc + kTY - 1) / kTY, (Zc + kZChunk - 1) / kZChunk);
+  cudaStream_t st = as_stream(stream);
+  for (int l = 0; l < nol && iters > 0; ++l) {
+    float* m = maps + (size_t)l * V;
+    float* bufs[2] = {tmp0, tmp1};
+    const float* src = m;
+    for (int it = 1; it <= iters; ++it) {
+      float* dst = (it == iters && it > 1) ? m : bufs[it & 1];
+      smooth_tile_kernel<false><<<tgrid, tblock, 0, st>>>(src, dst, Zc, Yc, Xc);
+      src = dst;
+    }
+    if (iters == 1 && cudaMemcpyAsync(m, src, V * sizeof(float), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_smooth_f32: copy failed");
+  }
+  return check_launch("si_smooth_f32");
+}

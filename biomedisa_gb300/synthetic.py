@@ -10,7 +10,8 @@ from numpy.random.default_rng(seed):
     interfaces; labels 0..8 on every 8th XY slice and every 16th YZ / XZ slice;
   * ``batch_volumes``  uneven uint16 volumes (64^3 .. 384x320x256) with 2..12
     phases and label spacing 4..20;
-  * ``large_volume``   1024^3 uint8 with 6 phases, labels on every 12th XY slice.
+  * ``large_volume``   1024^3 uint8 with 6 phases, uint8 labels on every 12th
+    XY slice.
 Each generator returns (image, sparse labels, ground truth).
 """
 from __future__ import annotations
@@ -72,9 +73,9 @@ def _render(truth, means, bg_mean, sigma, rng, blur=0.0, out_dtype=np.uint8, sca
     return np.rint(img).astype(out_dtype)
 
 
-def sparse_labels(truth, z_every=None, y_every=None, x_every=None):
+def sparse_labels(truth, z_every=None, y_every=None, x_every=None, dtype=np.int32):
     """Keeps the ground-truth labels on every n-th slice of each given axis."""
-    lab = np.zeros(truth.shape, np.int32)
+    lab = np.zeros(truth.shape, dtype)
     if z_every:
         lab[::z_every] = truth[::z_every]
     if y_every:
@@ -138,11 +139,77 @@ def batch_volumes(seed=0, count=32, lo=(64, 64, 64), hi=(256, 320, 384)):
     return out
 
 
-def large_volume(seed=0, shape=(1024, 1024, 1024), n_phases=6, z_every=12):
-    """Large case: 1024^3 uint8, 6 phases, labels on every 12th XY slice."""
+def large_volume(seed=0, shape=(1024, 1024, 1024), n_phases=6, z_every=12, slab=64):
+    """Large case: 1024^3 uint8, 6 phases, labels on every 12th XY slice.
+    Rendered in z-slabs to bound host memory."""
     rng = np.random.default_rng(seed)
     truth = np.zeros(shape, np.uint8)
     _phases(rng, truth, n_phases, size_frac=(0.1, 0.3))
     means = np.linspace(40, 220, n_phases).tolist()
-    img = _render(truth, means, 10, 12.0, rng)
-    return img, sparse_labels(truth, z_every=z_every), truth
+    lut = np.asarray([10] + list(means), np.float32)
+    img = np.empty(shape, np.uint8)
+    for z0 in range(0, shape[0], slab):
+        t = truth[z0:z0 + slab]
+        v = lut[t]
+        v += rng.normal(0.0, 12.0, size=t.shape).astype(np.float32)
+        np.clip(v, 0.0, 255.0, out=v)
+        img[z0:z0 + slab] = np.rint(v).astype(np.uint8)
+    return img, sparse_labels(truth, z_every=z_every, dtype=np.uint8), truth
+
+
+def _paint_shell(truth, label, center, semi, thickness, rot):
+    """An ellipsoidal shell: the ellipsoid minus a smaller concentric one."""
+    tmp = np.zeros_like(truth, dtype=bool)
+    inner = [max(s - thickness, 1.0) for s in semi]
+    t = np.zeros(truth.shape, np.uint8)
+    _paint_ellipsoid(t, 1, center, semi, rot)
+    _paint_ellipsoid(t, 2, center, inner, rot)
+    tmp[t == 1] = True
+    truth[tmp] = label
+
+
+def smooth_noise(rng, shape, octaves=3, base=8):
+    """Multi-octave smooth noise in [-1, 1] (sum of upsampled random lattices,
+    each octave twice as fine and half as strong)."""
+    from scipy.ndimage import zoom
+
+    out = np.zeros(shape, np.float32)
+    amp, total = 1.0, 0.0
+    for o in range(octaves):
+        cells = [max(2, s // (base >> o) if (base >> o) else s) for s in shape]
+        lat = rng.uniform(-1, 1, cells).astype(np.float32)
+        up = zoom(lat, [s / c for s, c in zip(shape, cells)], order=1)[: shape[0], : shape[1], : shape[2]]
+        out[: up.shape[0], : up.shape[1], : up.shape[2]] += amp * up
+        total += amp
+        amp *= 0.5
+    return out / total
+
+
+def procedural_volume(rng, shape=(96, 96, 96)):
+    """Training volume: 2-8 phases of random ellipsoids, tubes and shells,
+    smooth multi-octave intensity modulation, Gaussian noise sigma 5-25, uint8;
+    labels on every k-th z-slice, k in 6..14."""
+    n_ph = int(rng.integers(2, 9))
+    truth = np.zeros(shape, np.uint8)
+    n = min(shape)
+    for lab in range(1, n_ph + 1):
+        kind = rng.random()
+        if kind < 0.45:
+            s = rng.uniform(0.1 * n, 0.3 * n, 3)
+            c = [rng.uniform(0.15 * d, 0.85 * d) for d in shape]
+            _paint_ellipsoid(truth, lab, c, s, _rotation(rng))
+        elif kind < 0.75:
+            p0 = [rng.uniform(0.05 * d, 0.95 * d) for d in shape]
+            p1 = [rng.uniform(0.05 * d, 0.95 * d) for d in shape]
+            _paint_tube(truth, lab, p0, p1, rng.uniform(0.03 * n, 0.1 * n))
+        else:
+            s = rng.uniform(0.15 * n, 0.35 * n, 3)
+            c = [rng.uniform(0.25 * d, 0.75 * d) for d in shape]
+            _paint_shell(truth, lab, c, s, rng.uniform(2.0, 0.1 * n), _rotation(rng))
+    means = rng.uniform(20, 235, n_ph + 1).astype(np.float32)
+    img = means[truth]
+    img *= 1.0 + 0.25 * smooth_noise(rng, shape)
+    img += rng.normal(0.0, rng.uniform(5, 25), size=shape).astype(np.float32)
+    np.clip(img, 0, 255, out=img)
+    every = int(rng.integers(6, 15))
+    return np.rint(img).astype(np.uint8), sparse_labels(truth, z_every=every), truth

@@ -271,6 +271,66 @@ int si_remap_labels(uint8_t* out, int Zc, int Yc, int Xc, int cz0, int cy0,
 int si_smooth(uint32_t* maps, float* tmp0, float* tmp1, int nol, int Zc,
               int Yc, int Xc, int iters, void* stream);
 
+/* si_smooth on float32 maps (in place); used for the hybrid's combined maps. */
+int si_smooth_f32(float* maps, float* tmp0, float* tmp1, int nol, int Zc,
+                  int Yc, int Xc, int iters, void* stream);
+
+/* ---- learned surrogate (no counterpart in the reference) ----
+ * Tensors are NDHWC; activations bfloat16, weights bfloat16 [27][cout][cin]
+ * (tap-major, tap = (dz+1)*9 + (dy+1)*3 + (dx+1)), biases and gradients fp32.
+ * Convolutions are 3x3x3, stride 1, zero padding = dilation. */
+
+/* y = relu?(conv(x, w) + bias + residual); bias/residual nullable; out_f32
+ * selects an fp32 output. cin: multiple of 16; cout: 16, 32, 48 or 64. */
+int si_nn_conv3d_fwd(const void* x, const void* w, const float* bias,
+                     const void* residual, void* y, int N, int D, int H,
+                     int W, int cin, int cout, int dil, int relu, int out_f32,
+                     void* stream);
+
+/* dw[27][cout][cin] += sum_v dy[v][co] x[v + off][ci]; db[cout] += sum_v dy
+ * (db nullable). (cout, cin) in {16, 32}^2. */
+int si_nn_conv3d_wgrad(const void* x, const void* dy, float* dw, float* db,
+                       int N, int D, int H, int W, int cin, int cout, int dil,
+                       void* stream);
+
+/* w_flipped[tap][ci][co] = w[26 - tap][co][ci] (data-gradient weights). */
+int si_nn_flip_weights(const void* w, void* w_flipped, int cout, int cin,
+                       void* stream);
+
+/* g = g * (y > 0) (+ add, nullable); n elements (bf16). */
+int si_nn_relu_bwd(void* g, const void* y, const void* add, int64_t n,
+                   void* stream);
+
+/* Soft-target cross entropy over the first nol of C fp32 logits per voxel:
+ * *loss += sum_v w_v sum_l -p_l log softmax_l; dlogits (bf16) =
+ * w_v (softmax - p) * scale. weight nullable (1). */
+int si_nn_xent(const float* logits, const float* target, const float* weight,
+               int64_t V, int C, int nol, float scale, void* dlogits,
+               float* loss, void* stream);
+
+/* AdamW step on fp32 params (bias-corrected, decoupled weight decay);
+ * p_bf16 (nullable) receives the bfloat16 copy. */
+int si_nn_adamw(float* p, const float* g, float* m, float* v, void* p_bf16,
+                int64_t n, float lr, float beta1, float beta2, float eps,
+                float wd, int step, void* stream);
+
+/* Surrogate input features of a box [z0, z0+Dt) x [y0, ..) x [x0, ..) of a
+ * uint8 working volume (D, H, W): bf16 [Dt][Ht][Wt][16] = I/255, signed
+ * distance to the nearest labelled z-slice / 16 clamped to [-1, 1], 1 on seed
+ * voxels (slot_map >= 0), then per label slot s = 0..12 the linear
+ * interpolation along z of [slot_map == s] between the labelled z-slices
+ * below and above. zinfo: float[D][4] = {distance, z_lo, z_hi, w_lo} (z_lo,
+ * z_hi = -1 when absent; 16-byte aligned). Outside the volume: distance 1,
+ * rest 0. */
+int si_nn_features(const uint8_t* img, const int16_t* slot_map,
+                   const float* zinfo, int D, int H, int W, int z0, int y0,
+                   int x0, int Dt, int Ht, int Wt, void* out, void* stream);
+
+/* Softmax of fp32 logits [Ds][H][W][16] over the first nol channels for slab
+ * planes [zb, ze), written planar into probs[nol][Zout][H][W] at plane zo. */
+int si_nn_probs(const float* logits, int Ds, int H, int W, int zb, int ze,
+                int nol, float* probs, int Zout, int zo, void* stream);
+
 /* Measurement probes (no counterpart in the reference; used by bench.py for
  * the walker's roofline denominators). si_probe_l2_read reads `bytes` of buf
  * `reps` times with L1-bypassing 16-byte loads (sink: one uint32, almost never

@@ -1,0 +1,169 @@
+"""Surrogate network kernels against the float64 oracle (gradient check), and
+a short training run whose loss must fall."""
+import numpy as np
+import pytest
+import torch
+
+import nn_oracle as NO
+from biomedisa_gb300 import surrogate as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf(a, dev):
+    return torch.from_numpy(np.asarray(a, np.float32)).to(dev).to(torch.bfloat16)
+
+
+def _np(t):
+    return t.float().cpu().numpy().astype(np.float64)
+
+
+def _conv(cin, cout, dil, rng, dev):
+    w = NO.bf16_round(rng.standard_normal((27, cout, cin)) * 0.2)
+    b = rng.standard_normal(cout) * 0.1
+    wt = torch.from_numpy(w.astype(np.float32)).to(dev)
+    c = S.Conv(cin, cout, dil, wt, torch.from_numpy(b.astype(np.float32)).to(dev), wt.to(torch.bfloat16),
+               torch.zeros_like(wt), torch.zeros(cout, device=dev))
+    return c, w, b
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.parametrize("cin,cout,dil,shape", [
+    (16, 16, 1, (2, 7, 9, 11)), (16, 16, 3, (1, 5, 6, 70)), (16, 16, 8, (2, 9, 4, 129)), (16, 32, 1, (2, 7, 9, 11)),
+    (32, 32, 2, (2, 7, 9, 11)), (32, 16, 4, (2, 7, 9, 11)), (32, 32, 1, (2, 7, 9, 11))])
+def test_conv_forward_dgrad_wgrad(cin, cout, dil, shape, cuda):
+    """16 -> 16 runs the dedicated C = 16 kernel (rows of 64 voxels: W = 70 and
+    129 leave partial chunks); the others the generic kernel."""
+    rng = np.random.default_rng(cin * 7 + cout + dil)
+    x = NO.bf16_round(rng.standard_normal(shape + (cin,)))
+    c, w, b = _conv(cin, cout, dil, rng, cuda)
+    xt = _bf(x, cuda)
+    # forward (fp32 output: only accumulation order differs)
+    y = S.conv_fwd(xt, c, shape, relu=False, out_f32=True)
+    exp = NO.conv_fwd(x, w, b, dil)
+    assert np.max(np.abs(_np(y) - exp)) <= 1e-4 * max(1.0, np.abs(exp).max())
+    # forward bf16 with residual + relu
+    res = NO.bf16_round(rng.standard_normal(shape + (cout,)))
+    yb = S.conv_fwd(xt, c, shape, relu=True, residual=_bf(res, cuda))
+    expb = NO.bf16_round(np.maximum(exp + res, 0))
+    assert np.max(np.abs(_np(yb) - expb) / (np.abs(expb) + 1e-2)) <= 2 ** -7
+    # data gradient through the flipped weights
+    dy = NO.bf16_round(rng.standard_normal(shape + (cout,)))
+    dx = S.conv_dgrad(_bf(dy, cuda), c, shape)
+    assert _rel(_np(dx), NO.conv_dgrad(dy, w, dil)) < 1e-2
+    # weight and bias gradients (fp32)
+    c.gw.zero_()
+    c.gb.zero_()
+    S.conv_wgrad(xt, _bf(dy, cuda), c, shape)
+    assert _rel(c.gw.cpu().numpy().astype(np.float64), NO.conv_wgrad(x, dy, dil)) < 1e-5
+    assert _rel(c.gb.cpu().numpy().astype(np.float64), dy.reshape(-1, cout).sum(0)) < 1e-5
+
+
+def test_network_gradient_check(cuda):
+    """Whole network (stem, 2 residual blocks, head): loss, logits and every
+    layer's weight/bias gradient against the oracle."""
+    rng = np.random.default_rng(5)
+    net = S.SurrogateNet(channels=16, dilations=(1, 2), seed=3)
+    for c in net.convs:  # bf16-exact master weights so both sides start equal
+        c.w.copy_(c.wb.float())
+    shape = (1, 8, 10, 9)
+    x = NO.bf16_round(rng.uniform(0, 1, shape + (16,)) * (rng.random(shape + (16,)) < 0.5))
+    nol = 3
+    p = rng.dirichlet(np.ones(nol), size=shape)
+    wgt = (rng.random(shape) < 0.9).astype(np.float64)
+    logits = net.forward(_bf(x, cuda), keep=True)
+    loss, dl = net.loss_and_grad(logits, torch.from_numpy(p.astype(np.float32)).to(cuda),
+                                 torch.from_numpy(wgt.astype(np.float32)).to(cuda), nol)
+    net.zero_grad()
+    net.backward(dl)
+    ws = [c.w.cpu().numpy().astype(np.float64) for c in net.convs]
+    bs = [c.b.cpu().numpy().astype(np.float64) for c in net.convs]
+    e_loss, e_logits, dws, dbs = NO.network_grads(x, ws, bs, list(net.dilations), p, wgt, nol)
+    assert abs(float(loss) - e_loss) <= 1e-3 * abs(e_loss) + 1e-6
+    assert _rel(_np(logits), e_logits) < 1e-2
+    for k, c in enumerate(net.convs):
+        assert _rel(c.gw.cpu().numpy().astype(np.float64), dws[k]) < 3e-2, f"layer {k} dW"
+        assert _rel(c.gb.cpu().numpy().astype(np.float64), dbs[k]) < 3e-2, f"layer {k} db"
+
+
+def test_training_reduces_loss(cuda):
+    """AdamW on a fixed batch: the loss falls below 60 % of its start in 60 steps."""
+    rng = np.random.default_rng(8)
+    net = S.SurrogateNet(channels=16, dilations=(1, 2), seed=1)
+    shape = (2, 16, 16, 16)
+    x = rng.uniform(0, 1, shape + (16,))
+    x[..., 4:] = 0
+    lab = (x[..., 0] > 0.5).astype(np.int64)
+    nol = 2
+    p = np.eye(nol)[lab]
+    xt = _bf(x, cuda)
+    pt = torch.from_numpy(p.astype(np.float32)).to(cuda)
+    losses = []
+    for _ in range(60):
+        logits = net.forward(xt, keep=True)
+        loss, dl = net.loss_and_grad(logits, pt, None, nol)
+        net.zero_grad()
+        net.backward(dl)
+        net.adamw(lr=5e-3)
+        losses.append(float(loss))
+    assert losses[-1] < 0.6 * losses[0], losses
+
+
+def _job(img, lab, dev):
+    from biomedisa_gb300.interpolation import DeviceJob, _IMG_DTYPES, _LAB_DTYPES, upload
+    ti, tl = upload(img, lab, device=dev)
+    job = DeviceJob(ti, _IMG_DTYPES[img.dtype], tl, _LAB_DTYPES[lab.dtype])
+    assert job.analyze() is None
+    job.prepare()
+    return job
+
+
+def test_features_and_slot_map(cuda):
+    """Feature channels against a NumPy restatement; the slot map comes from
+    the seed records (every labelled-slice voxel of a plain volume)."""
+    from biomedisa_gb300 import synthetic as syn
+    img, lab, _ = syn.plain_volume(seed=2, shape=(40, 36, 44), z_every=7, semi=(6, 14))
+    job = _job(img, lab, cuda)
+    cp = job.cplan
+    sm = S.slot_map_of(job).cpu().numpy()
+    f = S.features(job, -3, 2, -1, (cp.Zc + 4, cp.Yc - 3, cp.Xc)).float().cpu().numpy()[0]
+    work = job.work.view(cp.Zc, cp.Yc, cp.Xc).cpu().numpy()
+    zs = sorted(s for a, s in cp.slice_list.tolist() if a == 0)
+    tab = S.slice_table(cp.Zc, zs)
+    exp = np.zeros_like(f)
+    exp[..., 1] = 1.0
+    ys, xs = slice(2, 2 + f.shape[1]), slice(0, cp.Xc - 1)
+    for zt in range(f.shape[0]):
+        z = zt - 3
+        if not 0 <= z < cp.Zc:
+            continue
+        exp[zt, :, 1:, 0] = work[z, ys, xs] / 255.0
+        exp[zt, :, 1:, 1] = np.clip(tab[z, 0] / 16.0, -1, 1)
+        exp[zt, :, 1:, 2] = sm[z, ys, xs] >= 0
+        lo, hi, w = int(tab[z, 1]), int(tab[z, 2]), float(tab[z, 3])
+        slo = sm[lo, ys, xs] if lo >= 0 else np.full((f.shape[1], cp.Xc - 1), -1)
+        shi = sm[hi, ys, xs] if hi >= 0 else np.full((f.shape[1], cp.Xc - 1), -1)
+        for k in range(13):
+            exp[zt, :, 1:, 3 + k] = np.float32(w) * (slo == k) + np.float32(1 - w) * (shi == k)
+    assert np.max(np.abs(f - NO.bf16_round(exp))) == 0.0
+    # seeds: every voxel of a labelled z-slice inside the volume (the crop
+    # of this small volume spans the one-voxel padding frame too)
+    for z in zs:
+        assert (sm[z, 1:-1, 1:-1] >= 0).all() and (sm[z, 0] == -1).all() and (sm[z, :, -1] == -1).all()
+    assert (sm[[z for z in range(cp.Zc) if z not in zs]] == -1).all()
+
+
+def test_slab_inference_matches_single_pass(cuda):
+    """z-slabs with a receptive-radius halo reproduce one pass over the crop bit for bit."""
+    from biomedisa_gb300 import synthetic as syn
+    img, lab, _ = syn.plain_volume(seed=4, shape=(70, 40, 48), z_every=9, semi=(8, 16))
+    job = _job(img, lab, cuda)
+    net = S.SurrogateNet(channels=16, dilations=(1, 2, 4, 8), seed=2)
+    whole = S.predict(net, job, slab=job.cplan.Zc)
+    for slab in (5, 17, 33):
+        part = S.predict(net, job, slab=slab)
+        assert torch.equal(part, whole), slab
+    assert torch.allclose(whole.sum(0), torch.ones_like(whole[0]), atol=1e-5)
