@@ -13,7 +13,7 @@ and outputs (host->device copies and result download inside the timed region).
 ``--impl reference`` times the reference's own CPU walker on the host cores.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                       [--workload allaxis|plain|large]
+                       [--workload allaxis|plain|batch|large|train|hybrid]
 """
 from __future__ import annotations
 
@@ -43,7 +43,18 @@ WORKLOADS = {
                   allaxis=False),
     "large": dict(desc="large uint8 1024^3, 6 phases, labels every 12th z-slice, nbrw=10, sorw=4000, smooth=100",
                   nbrw=10, sorw=4000, smooth=100, allaxis=False),
+    "train": dict(desc="surrogate training: residual 3-D CNN (16 channels, dilations 1,2,4,8, 70 k parameters), "
+                       "bf16 activations/weights with fp32 accumulation, batch 8 windows of 64^3 from 16 walked "
+                       "128^3 volumes (procedural and large-style), soft-target cross entropy, AdamW",
+                  nbrw=10, sorw=4000, smooth=0, allaxis=False),
+    "hybrid": dict(desc="hybrid vs plain on the large uint8 1024^3 volume (6 phases, labels every 12th z-slice, "
+                        "nbrw=10, sorw=4000, smooth=0): surrogate everywhere, walk from the seeds within 8 voxels "
+                        "of voxels with max p < 0.97 (grown by 2); judge = the full plain walk",
+                   nbrw=10, sorw=4000, smooth=0, allaxis=False, threshold=0.97, radius=8, coarse=4, grow=2),
 }
+
+# one kernel per entry-point call except these (launches per call)
+MULTI_LAUNCH = {"si_extract_seeds": 3, "si_nn_conv3d_wgrad": 2}
 
 WALK_SECTORS_L2 = 2  # per walker step at L2: one packed-record sector + one atomic sector
 WALK_BYTES_PAYLOAD_U8 = 10  # 6 neighbour bytes + one 4-byte hit per step
@@ -197,6 +208,28 @@ def run_job(img_t, img_code, lab_t, lab_code, wl, events=None):
     return job, res
 
 
+def reference_seed_count(lab):
+    """Seeds the reference walks for a z-slice-labelled volume: interior
+    voxels of the labelled slices of its crop whose label is walked
+    (oracle restatement of pre_processing, predict_blocksize and
+    read_labeled_slices)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    labelData, all_labels = oracle.pre_processing(lab)
+    labelData = np.pad(labelData, 1)
+    az, bz, ay, by, ax, bx = oracle.predict_blocksize(labelData)
+    labc = labelData[az:bz, ay:by, ax:bx]
+    zs = oracle.read_labeled_slices(labc)[0]
+    walked = np.zeros(256 + 1, bool)
+    walked[np.asarray(all_labels, np.int64)] = True
+    n = 0
+    for z in zs:
+        v = labc[z, 1:-1, 1:-1].astype(np.int64)
+        n += int(walked[np.clip(v, 0, 256)][(v >= 0) & (v <= 255)].sum())
+    return n
+
+
 def cpu_baseline(img, lab, wl, target_seconds):
     """The reference's OpenCL walker compiled as C on a bounded sample of this
     workload (same crop/working image the reference would walk)."""
@@ -268,6 +301,12 @@ def main():
         return
     if args.workload == "batch":
         run_batch_bench(args, wl)
+        return
+    if args.workload == "train":
+        run_train_bench(args, wl)
+        return
+    if args.workload == "hybrid":
+        run_hybrid_bench(args, wl)
         return
     if args.impl == "reference":
         run_reference(args, wl)
@@ -451,6 +490,305 @@ def run_batch_bench(args, wl):
                 "d2h_bytes_per_step": int(sum(v.nbytes for r in out if r for v in r.values()))},
         "clocks": clocks.summary(),
     }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def launches_since(before, sweeps=0):
+    """Kernel launches of libsmartinterp calls made since the `before`
+    snapshot of _native.CALLS (si_walk_sorted: 6 per sweep + 4)."""
+    from biomedisa_gb300 import _native as nat
+
+    n = 0
+    for k, v in nat.CALLS.items():
+        d = v - before.get(k, 0)
+        if k == "si_walk_sorted":
+            n += 6 * sweeps + 4 * d
+        else:
+            n += MULTI_LAUNCH.get(k, 1) * d
+    return n
+
+
+def peaks():
+    pk = ROOT / "MEASURED_PEAKS.json"
+    return json.loads(pk.read_text()) if pk.exists() else {}
+
+
+def surrogate_samples(count=16, shape=(128, 128, 128)):
+    from biomedisa_gb300 import surrogate as SG
+
+    return SG.training_set(count, shape=shape, mix=0.5, seed=7)
+
+
+def trained_surrogate():
+    """The hybrid's network: trained here (128 walked 96^3 volumes, 70 %
+    large-style, 5000 AdamW steps on batches of 4 windows) or read back from the
+    bench cache directory."""
+    import torch
+
+    from biomedisa_gb300 import surrogate as SG
+
+    cache = Path(os.environ.get("SI_BENCH_CACHE", "/tmp")) / "si_surrogate_c16_d1248_n128_s5000_v2.pt"
+    if cache.exists():
+        return SG.load(cache), {"trained": False, "cache": str(cache)}
+    t0 = time.perf_counter()
+    net = SG.SurrogateNet(seed=0)
+    samples = SG.training_set(128, mix=0.7, seed=0)
+    t1 = time.perf_counter()
+    losses = SG.train(net, samples, 5000, seed=0)
+    torch.cuda.synchronize()
+    info = {"trained": True, "samples_s": t1 - t0, "train_s": time.perf_counter() - t1,
+            "loss_first100": float(np.mean(losses[:100])), "loss_last100": float(np.mean(losses[-100:]))}
+    try:
+        SG.save(net, cache)
+    except OSError:
+        pass
+    return net, info
+
+
+def nn_cpu_baseline(net, target_seconds=10.0):
+    """The float64 NumPy oracle's forward + backward of the same network on
+    one 32^3 window, repeated for about target_seconds (1 core)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import nn_oracle as NO
+
+    rng = np.random.default_rng(0)
+    n = 32
+    x = NO.bf16_round(rng.uniform(0, 1, (1, n, n, n, 16)))
+    ws = [c.w.cpu().numpy().astype(np.float64) for c in net.convs]
+    bs = [c.b.cpu().numpy().astype(np.float64) for c in net.convs]
+    p = rng.dirichlet(np.ones(4), size=(1, n, n, n))
+    w = np.ones((1, n, n, n))
+    t0, reps = time.perf_counter(), 0
+    while True:
+        NO.network_grads(x, ws, bs, list(net.dilations), p, w, 4)
+        reps += 1
+        if time.perf_counter() - t0 >= target_seconds:
+            break
+    secs = time.perf_counter() - t0
+    return {"value": reps * n ** 3 / secs, "unit": "voxels/s", "cores": 1, "kind": "port",
+            "sample": f"{reps} forward+backward passes of one 32^3 window through the float64 NumPy oracle "
+                      f"(oracle/nn_oracle.py network_grads), {secs:.1f} s"}
+
+
+def run_train_bench(args, wl):
+    """Surrogate training throughput: one step = forward, backward and AdamW
+    over a batch of 8 windows of 64^3 (device-resident training set)."""
+    import torch
+
+    from biomedisa_gb300 import _native as nat
+    from biomedisa_gb300 import surrogate as SG
+
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned surrogate; nothing "
+                              "to train"}))
+        return
+    world, rank, local = dist_setup()
+    samples = surrogate_samples()
+    net = SG.SurrogateNet(seed=0)
+    batch, patch = 8, 64
+    for i in range(args.warmup):
+        SG.train(net, samples, 1, batch=batch, patch=patch, seed=100 + i)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    l2buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    times, launches = [], 0
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            flush_l2(l2buf)
+            torch.cuda.synchronize()
+            barrier(world)
+            before = dict(nat.CALLS)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            SG.train(net, samples, 1, batch=batch, patch=patch, seed=200 + i)
+            e.record(stream)
+            torch.cuda.synchronize()
+            barrier(world)
+            times.append(s.elapsed_time(e))
+            launches = launches_since(before)
+    ms = max_over_ranks(world, sum(times) / len(times))
+    vox = batch * patch ** 3
+    value = world * vox / (ms / 1e3)
+    # conv roofline: every conv runs forward, data gradient (except the stem) and weight gradient
+    flops = 0
+    for k, c in enumerate(net.convs):
+        per = 2 * 27 * c.cin * c.cout * vox
+        flops += per * (3 if k > 0 else 2)
+    # per-kernel CUDA-event timing of the 16->16 forward convolution on one batch
+    x = torch.randn((batch, patch, patch, patch, 16), device="cuda").to(torch.bfloat16)
+    c = net.convs[1]
+    shape = (batch, patch, patch, patch)
+    for _ in range(3):
+        SG.conv_fwd(x, c, shape, relu=True)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for _ in range(20):
+        SG.conv_fwd(x, c, shape, relu=True)
+    e.record(stream)
+    torch.cuda.synchronize()
+    conv_ms = s.elapsed_time(e) / 20
+    conv_tflops = 2 * 27 * 16 * 16 * vox / (conv_ms / 1e3) / 1e12
+    pk = peaks()
+    bf16 = float(pk.get("bf16_tflops", 1900.0))
+    kind = "measured" if "bf16_tflops" in pk else "fallback"
+    e2e_t = []
+    for i in range(args.e2e_steps or args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        SG.train(net, samples, 1, batch=batch, patch=patch, seed=300 + i)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(world, sum(e2e_t) / len(e2e_t))
+    line = {
+        "metric": "training voxels/s", "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16", "data": "synthetic (walked procedural volumes; targets = hit fractions of the walk)",
+        "config": {"workload": wl["desc"], "global_batch": batch, "seq_len": patch ** 3,
+                   "parallelism": "single GPU", "l2": "256 MiB buffer written before every timed step"},
+        "step_tflops": flops / (ms / 1e3) / 1e12,
+        "e2e": {"value": world * vox / e2e_s, "unit": "voxels/s", "seconds": e2e_s, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 4,
+                "note": "the public training call (surrogate.train) on the device-resident training set; the loss "
+                        "(4 bytes) is read back each step"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "tensor", "achieved": conv_tflops, "peak": bf16, "unit": "TFLOP/s",
+                     "frac": conv_tflops / bf16, "traffic": None,
+                     "note": f"16->16 forward convolution (conv16_kernel, mma.sync bf16), 2*27*16*16 FLOP per "
+                             f"output voxel x {vox} voxels / CUDA-event time; peak {kind} bf16 (cuBLAS burst)"},
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = nn_cpu_baseline(net, min(args.ref_seconds, 20.0))
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def run_hybrid_bench(args, wl):
+    """Hybrid (surrogate + restricted walk) vs the plain job on the large
+    volume; value = voxels/s of the hybrid on device-resident inputs."""
+    import torch
+
+    from biomedisa_gb300 import _native as nat
+    from biomedisa_gb300 import interpolation as I
+    from biomedisa_gb300 import surrogate as SG
+
+    if args.impl == "reference":
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        img, lab = make_inputs("large")
+        cb = cpu_baseline(img, lab, wl, args.ref_seconds)
+        line = {"metric": "voxels/s", "unit": "voxels/s", "impl": "reference"}
+        # the reference walks every seed: extrapolate its walker rate to the whole plain walk
+        seeds_total = reference_seed_count(lab)
+        secs = seeds_total * wl["nbrw"] * wl["sorw"] / cb["value"]
+        v = int(np.prod(img.shape)) / secs
+        line.update(value=v, n_gpus=world, steps=args.steps, warmup=args.warmup, ms_per_step=secs * 1e3,
+                    higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
+                    config={"workload": wl["desc"], "global_batch": 1, "parallelism": "host cores"},
+                    cpu_baseline={"value": v, "unit": "voxels/s", "cores": cb["cores"], "kind": "reference",
+                                  "sample": cb["sample"] + f"; extrapolated to all {seeds_total} seeds"},
+                    e2e={"value": v, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
+        print(json.dumps(line))
+        return
+    world, rank, local = dist_setup()
+    img, lab = make_inputs("large")
+    net, train_info = trained_surrogate()
+    data, labels = I.normalize_host_dtypes(img, lab)
+    icode, lcode = I._IMG_DTYPES[data.dtype], I._LAB_DTYPES[labels.dtype]
+    img_t, lab_t = I.upload(data, labels)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    # the judge: one plain job (same entry points as the large workload, smooth=0)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record(stream)
+    job, res = run_job(img_t, icode, lab_t, lcode, wl)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    plain_ms = ev[0].elapsed_time(ev[1])
+    plain = res["regular"]
+    plain_steps = job.total_steps()
+    present = sorted(int(v) for v in np.unique(lab[::12]))
+    del job, res
+    torch.cuda.empty_cache()
+    kw = dict(threshold=wl["threshold"], radius=wl["radius"], coarse=wl["coarse"], grow=wl["grow"],
+              nbrw=wl["nbrw"], sorw=wl["sorw"])
+    for _ in range(args.warmup):
+        r, _ = SG.hybrid_interpolation(None, None, net, device_inputs=(img_t, icode, lab_t, lcode), **kw)
+        del r
+    torch.cuda.synchronize()
+    l2buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    times, launches, st, dice = [], 0, {}, {}
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush_l2(l2buf)
+            torch.cuda.synchronize()
+            barrier(world)
+            before = dict(nat.CALLS)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            r, st = SG.hybrid_interpolation(None, None, net, device_inputs=(img_t, icode, lab_t, lcode), **kw)
+            e.record(stream)
+            torch.cuda.synchronize()
+            barrier(world)
+            times.append(s.elapsed_time(e))
+            launches = launches_since(before, st["sweeps"])
+            dice = SG.label_dice(r["regular"], plain, present)
+            del r
+    ms = max_over_ranks(world, sum(times) / len(times))
+    vox = int(np.prod(img.shape))
+    # end to end: host arrays in, host labels out
+    t_e2e = []
+    out_bytes = 0
+    for _ in range(args.e2e_steps or args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r, _ = SG.hybrid_interpolation(img, lab, net, **kw)
+        out = r["regular"].cpu().numpy()
+        t_e2e.append(time.perf_counter() - t0)
+        out_bytes = out.nbytes
+        del r
+    e2e_s = max_over_ranks(world, sum(t_e2e) / len(t_e2e))
+    pk = peaks()
+    hbm = float(pk.get("hbm_gbs", 6800.0))
+    kind = "measured" if "hbm_gbs" in pk else "fallback"
+    walk_rate = st["walker_steps"] / (st["walk_ms_events"] / 1e3) if st.get("walk_ms_events") else None
+    achieved = walk_rate * WALK_BYTES_PAYLOAD_U8 / 1e9 if walk_rate else None
+    line = {
+        "metric": "voxels/s", "value": world * vox / (ms / 1e3), "unit": "voxels/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded generator, no public dataset)",
+        "config": {"workload": wl["desc"], "global_batch": 1, "parallelism": "single GPU",
+                   "l2": "256 MiB buffer written before every timed step; hit maps 30 GB > L2"},
+        "plain_ms": plain_ms, "plain_voxels_per_s": vox / (plain_ms / 1e3), "speedup_vs_plain": plain_ms / ms,
+        "dice_vs_plain": {str(k): round(v, 5) for k, v in dice.items()},
+        "dice_min": min(dice.values()) if dice else None,
+        "frac_uncertain": st.get("frac_uncertain"), "frac_seeds_walked": st.get("frac_seeds_walked"),
+        "walker_steps": st.get("walker_steps"), "plain_walker_steps": plain_steps,
+        "seconds_surrogate": st.get("seconds_surrogate"), "seconds_walk": st.get("seconds_walk"),
+        "surrogate": train_info,
+        "e2e": {"value": world * vox / e2e_s, "unit": "voxels/s", "seconds": e2e_s,
+                "h2d_bytes_per_step": int(img.nbytes + lab.nbytes), "d2h_bytes_per_step": int(out_bytes)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm if achieved else None, "traffic": None,
+                     "note": f"restricted walk (sweep_kernel): {WALK_BYTES_PAYLOAD_U8} B/step logical payload x "
+                             f"steps / CUDA-event walk time; peak {kind} (hbm_gbs)"},
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cb = cpu_baseline(img, lab, wl, args.ref_seconds)
+            secs = plain_steps / cb["value"]
+            line["cpu_baseline"] = {"value": vox / secs, "unit": "voxels/s", "cores": cb["cores"],
+                                    "kind": "reference",
+                                    "sample": cb["sample"] + f"; extrapolated to the plain walk's {plain_steps} "
+                                                             "steps"}
+        except Exception as ex:
+            line["cpu_baseline"] = {"value": None, "unit": "voxels/s", "cores": 0, "kind": "reference",
+                                    "sample": f"unavailable: {ex}"}
     if rank == 0:
         print(json.dumps(line))
 

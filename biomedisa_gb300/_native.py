@@ -52,8 +52,9 @@ _SIGNATURES = {
     "si_probe_l2_atomics": [_c_void_p, _c_u64, _c_u64, _c_void_p],
     "si_nn_conv3d_fwd": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int,
                          _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_nn_wgrad_partial_bytes": [_c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
     "si_nn_conv3d_wgrad": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int,
-                           _c_int, _c_int, _c_void_p],
+                           _c_int, _c_int, _c_void_p, _c_u64, _c_void_p],
     "si_nn_flip_weights": [_c_void_p, _c_void_p, _c_int, _c_int, _c_void_p],
     "si_nn_relu_bwd": [_c_void_p, _c_void_p, _c_void_p, ctypes.c_int64, _c_void_p],
     "si_nn_xent": [_c_void_p, _c_void_p, _c_void_p, ctypes.c_int64, _c_int, _c_int, _c_float, _c_void_p, _c_void_p,
@@ -103,9 +104,13 @@ def lib() -> ctypes.CDLL:
     return _lib
 
 
+CALLS: dict[str, int] = {}  # entry-point call counts (measurement bookkeeping)
+
+
 def call(name: str, *args) -> None:
     """Calls an entry point and raises NativeError on a non-zero status."""
     L = lib()
+    CALLS[name] = CALLS.get(name, 0) + 1
     rc = getattr(L, name)(*args)
     if rc != 0:
         msg = L.si_last_error().decode(errors="replace")

@@ -318,7 +318,8 @@ __device__ __forceinline__ void ldsm_x4_trans(uint32_t (&r)[4], uint32_t addr) {
 
 __global__ void __launch_bounds__(128) wgrad16_kernel(const __nv_bfloat16* __restrict__ x,
                                                       const __nv_bfloat16* __restrict__ dy, float* __restrict__ dw,
-                                                      Vol5 g, int dil, int xchunks, int64_t rows_per_block) {
+                                                      float* __restrict__ partials, Vol5 g, int dil, int xchunks,
+                                                      int64_t rows_per_block) {
   __shared__ __align__(16) uint8_t s_dy[64 * 32];
   __shared__ __align__(16) uint8_t s_x[4][64 * 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -391,14 +392,20 @@ __global__ void __launch_bounds__(128) wgrad16_kernel(const __nv_bfloat16* __res
   for (int i = 0; i < 7; ++i) {
     const int tap = warp + 4 * i;
     if (tap >= 27) break;
-    float* d = dw + tap * 256;
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
       const int ci = j * 8 + tig * 2;
-      atomicAdd(&d[grp * 16 + ci], acc[i][j][0]);
-      atomicAdd(&d[grp * 16 + ci + 1], acc[i][j][1]);
-      atomicAdd(&d[(grp + 8) * 16 + ci], acc[i][j][2]);
-      atomicAdd(&d[(grp + 8) * 16 + ci + 1], acc[i][j][3]);
+      if (partials) {  // deterministic: this block's sums, reduced in block order by reduce_partials_kernel
+        float* d = partials + ((int64_t)blockIdx.x * 27 + tap) * 256;
+        *reinterpret_cast<float2*>(&d[grp * 16 + ci]) = make_float2(acc[i][j][0], acc[i][j][1]);
+        *reinterpret_cast<float2*>(&d[(grp + 8) * 16 + ci]) = make_float2(acc[i][j][2], acc[i][j][3]);
+      } else {
+        float* d = dw + tap * 256;
+        atomicAdd(&d[grp * 16 + ci], acc[i][j][0]);
+        atomicAdd(&d[grp * 16 + ci + 1], acc[i][j][1]);
+        atomicAdd(&d[(grp + 8) * 16 + ci], acc[i][j][2]);
+        atomicAdd(&d[(grp + 8) * 16 + ci + 1], acc[i][j][3]);
+      }
     }
   }
 }
@@ -415,10 +422,14 @@ __global__ void flip_weights_kernel(const __nv_bfloat16* __restrict__ w, __nv_bf
   }
 }
 
-// bias gradient: db[c] += sum_v dy[v][c]
+// bias gradient: db[c] += sum_v dy[v][c]. Each thread sums a fixed set of
+// voxels, warps reduce by shuffles and the block's warps in order; with
+// `partials` the block writes its sums (reduced in block order afterwards),
+// otherwise it adds them to db atomically.
 template <int kC>
 __global__ void __launch_bounds__(256) bias_grad_kernel(const __nv_bfloat16* __restrict__ dy, int64_t V,
-                                                        float* __restrict__ db) {
+                                                        float* __restrict__ db, float* __restrict__ partials) {
+  __shared__ float s_sum[8][kC];
   float acc[kC];
 #pragma unroll
   for (int c = 0; c < kC; ++c) acc[c] = 0.0f;
@@ -427,11 +438,31 @@ __global__ void __launch_bounds__(256) bias_grad_kernel(const __nv_bfloat16* __r
 #pragma unroll
     for (int c = 0; c < kC; ++c) acc[c] += __bfloat162float(row[c]);
   }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int c = 0; c < kC; ++c) {
     float s = acc[c];
     for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&db[c], s);
+    if (lane == 0) s_sum[warp][c] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < kC) {
+    float s = 0.0f;
+    for (int w = 0; w < 8; ++w) s += s_sum[w][threadIdx.x];
+    if (partials)
+      partials[(int64_t)blockIdx.x * kC + threadIdx.x] = s;
+    else
+      atomicAdd(&db[threadIdx.x], s);
+  }
+}
+
+// out[i] += sum_b partials[b][i], b ascending (n outputs, nb blocks)
+__global__ void __launch_bounds__(256) reduce_partials_kernel(const float* __restrict__ partials, int nb, int n,
+                                                              float* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float s = 0.0f;
+    for (int b = 0; b < nb; ++b) s += partials[(int64_t)b * n + i];
+    out[i] += s;
   }
 }
 
@@ -632,8 +663,20 @@ extern "C" int si_nn_conv3d_fwd(const void* x, const void* w, const float* bias,
   return check_launch("si_nn_conv3d_fwd");
 }
 
+extern "C" int si_nn_wgrad_partial_bytes(int N, int D, int H, int W, int cin, int cout, uint64_t* bytes) {
+  clear_error();
+  if (!bytes || N < 1 || D < 1 || H < 1 || W < 1 || cin < 1 || cout < 1)
+    return set_error(SI_ERR_ARG, "si_nn_wgrad_partial_bytes: bad arguments");
+  const int64_t V = (int64_t)N * D * H * W;
+  const int64_t wblocks = (int64_t)sm_count() * 8;
+  const int64_t bblocks = egrid(V);
+  *bytes = (uint64_t)(wblocks * 27 * cout * cin + bblocks * cout) * sizeof(float);
+  return 0;
+}
+
 extern "C" int si_nn_conv3d_wgrad(const void* x, const void* dy, float* dw, float* db, int N, int D, int H, int W,
-                                  int cin, int cout, int dil, void* stream) {
+                                  int cin, int cout, int dil, float* partials, uint64_t partial_bytes,
+                                  void* stream) {
   clear_error();
   if (!x || !dy || !dw) return set_error(SI_ERR_ARG, "si_nn_conv3d_wgrad: null pointer");
   if (N < 1 || D < 1 || H < 1 || W < 1 || dil < 1) return set_error(SI_ERR_ARG, "si_nn_conv3d_wgrad: bad shape");
@@ -644,21 +687,34 @@ extern "C" int si_nn_conv3d_wgrad(const void* x, const void* dy, float* dw, floa
   const auto* xb = static_cast<const __nv_bfloat16*>(x);
   const auto* db16 = static_cast<const __nv_bfloat16*>(dy);
   const bool aligned = ((uintptr_t)x % 16 == 0) && ((uintptr_t)dy % 16 == 0);
-  if (cout == 16 && cin == 16 && aligned) {
+  const bool fast = cout == 16 && cin == 16 && aligned;
+  if (partials) {
+    uint64_t need = 0;
+    si_nn_wgrad_partial_bytes(N, D, H, W, cin, cout, &need);
+    if (!fast) return set_error(SI_ERR_ARG, "si_nn_conv3d_wgrad: deterministic partials need cin = cout = 16");
+    if (partial_bytes < need || (uintptr_t)partials % 16)
+      return set_error(SI_ERR_ARG, "si_nn_conv3d_wgrad: partials buffer too small or misaligned");
+  }
+  if (fast) {
     const int xchunks = (W + 63) / 64;
     const int64_t rows = (int64_t)N * D * H * xchunks;
     const int64_t want = (int64_t)sm_count() * 8;
     const int64_t per = (rows + want - 1) / want;
     const int64_t blocks = (rows + per - 1) / per;
-    wgrad16_kernel<<<(unsigned)blocks, 128, 0, st>>>(xb, db16, dw, g, dil, xchunks, per);
+    wgrad16_kernel<<<(unsigned)blocks, 128, 0, st>>>(xb, db16, dw, partials, g, dil, xchunks, per);
+    if (partials)
+      reduce_partials_kernel<<<(27 * 256 + 255) / 256, 256, 0, st>>>(partials, (int)blocks, 27 * 256, dw);
   } else if (cout == 16 && cin == 16) conv3d_wgrad_kernel<16, 16><<<grid, 128, 0, st>>>(xb, db16, dw, g, dil);
   else if (cout == 32 && cin == 16) conv3d_wgrad_kernel<32, 16><<<grid, 128, 0, st>>>(xb, db16, dw, g, dil);
   else if (cout == 16 && cin == 32) conv3d_wgrad_kernel<16, 32><<<grid, 128, 0, st>>>(xb, db16, dw, g, dil);
   else if (cout == 32 && cin == 32) conv3d_wgrad_kernel<32, 32><<<grid, 128, 0, st>>>(xb, db16, dw, g, dil);
   else return set_error(SI_ERR_ARG, "si_nn_conv3d_wgrad: (cout, cin) must be in {16, 32}^2");
   if (db) {
-    if (cout == 16) bias_grad_kernel<16><<<egrid(V), 256, 0, st>>>(db16, V, db);
-    else bias_grad_kernel<32><<<egrid(V), 256, 0, st>>>(db16, V, db);
+    const int bb = egrid(V);
+    float* bpart = partials ? partials + (int64_t)sm_count() * 8 * 27 * cout * cin : nullptr;
+    if (cout == 16) bias_grad_kernel<16><<<bb, 256, 0, st>>>(db16, V, db, bpart);
+    else bias_grad_kernel<32><<<bb, 256, 0, st>>>(db16, V, db, bpart);
+    if (bpart) reduce_partials_kernel<<<1, 256, 0, st>>>(bpart, bb, cout, db);
   }
   return check_launch("si_nn_conv3d_wgrad");
 }

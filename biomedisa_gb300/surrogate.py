@@ -79,10 +79,33 @@ def conv_dgrad(dy, conv: Conv, shape, residual=None):
     return dx
 
 
-def conv_wgrad(x, dy, conv: Conv, shape):
+_PARTIALS: dict = {}
+
+
+def _partials(shape, cin, cout, device):
+    """Cached scratch for the deterministic 16-channel weight gradient."""
+    import ctypes
+
+    need = ctypes.c_uint64(0)
+    nat.call("si_nn_wgrad_partial_bytes", *shape, cin, cout, ctypes.byref(need))
+    key = str(device)
+    buf = _PARTIALS.get(key)
+    if buf is None or buf.numel() * 4 < need.value:
+        buf = torch.empty((int(need.value) + 3) // 4, dtype=torch.float32, device=device)
+        _PARTIALS[key] = buf
+    return buf
+
+
+def conv_wgrad(x, dy, conv: Conv, shape, deterministic=True):
+    """Adds the weight and bias gradients of one convolution to conv.gw /
+    conv.gb; 16 -> 16 convolutions reduce in a fixed order (deterministic)."""
     N, D, H, W = shape
+    part, nbytes = None, 0
+    if deterministic and conv.cin == 16 and conv.cout == 16:
+        buf = _partials(shape, conv.cin, conv.cout, x.device)
+        part, nbytes = buf.data_ptr(), buf.numel() * 4
     nat.call("si_nn_conv3d_wgrad", _p(x), _p(dy), _p(conv.gw), _p(conv.gb), N, D, H, W, conv.cin, conv.cout,
-             conv.dil, _stream())
+             conv.dil, part, nbytes, _stream())
 
 
 def relu_bwd(g, y, add=None):
@@ -175,16 +198,20 @@ class SurrogateNet:
             nat.call("si_nn_adamw", _p(c.b), _p(c.gb), _p(c.mb), _p(c.vb), None, c.b.numel(), lr, beta1, beta2,
                      eps, 0.0, self.step_count, _stream())
 
-    def loss_and_grad(self, logits, target, weight, nol, extra_scale=1.0):
-        """Soft-target cross entropy (mean over weighted voxels); returns
-        (loss tensor, bf16 dlogits scaled by extra_scale / sum of weights)."""
+    def loss_and_grad(self, logits, target, weight, nol, extra_scale=1.0, denom=None):
+        """Soft-target cross entropy, summed over voxels (times their weight)
+        and divided by `denom` (default: the sum of the weights, which costs a
+        device synchronisation); returns (loss tensor, bf16 dlogits scaled by
+        extra_scale / denom)."""
         V = logits.numel() // OUT_CH
         dl = torch.empty(logits.shape, dtype=BF16, device=logits.device)
         loss = torch.zeros(1, dtype=torch.float32, device=logits.device)
-        wsum = float(weight.sum()) if weight is not None else float(V)
-        nat.call("si_nn_xent", _p(logits), _p(target), _p(weight), V, OUT_CH, nol,
-                 float(extra_scale) / max(wsum, 1.0), _p(dl), _p(loss), _stream())
-        return loss / max(wsum, 1.0), dl
+        if denom is None:
+            denom = float(weight.sum()) if weight is not None else float(V)
+        denom = max(float(denom), 1.0)
+        nat.call("si_nn_xent", _p(logits), _p(target), _p(weight), V, OUT_CH, nol, float(extra_scale) / denom, _p(dl),
+                 _p(loss), _stream())
+        return loss / denom, dl
 
     # ---- persistence --------------------------------------------------------
     def state_dict(self):
@@ -338,14 +365,20 @@ def make_sample(img, lab, nbrw=10, sorw=4000, rng_seed=None):
     return Sample(features(job), p, w, job.lplan.nol)
 
 
-def training_set(n, shape=(96, 96, 96), nbrw=10, sorw=4000, seed=0):
-    """n procedural volumes (synthetic.procedural_volume) with their targets."""
-    from .synthetic import procedural_volume
+def training_set(n, shape=(96, 96, 96), nbrw=10, sorw=4000, seed=0, mix=0.5):
+    """n training samples: procedural volumes (synthetic.procedural_volume)
+    and, for a fraction `mix`, volumes in the style of the large workload
+    (synthetic.large_volume: 6 phases, noise 12, labels every 12th z-slice)."""
+    from .synthetic import large_volume, procedural_volume
 
     rng = np.random.default_rng(seed)
     out = []
     while len(out) < n:
-        img, lab, _ = procedural_volume(rng, shape)
+        if rng.random() < mix:
+            img, lab, _ = large_volume(seed=int(rng.integers(1 << 30)), shape=shape, z_every=int(rng.integers(8, 15)))
+            lab = lab.astype(np.int32)
+        else:
+            img, lab, _ = procedural_volume(rng, shape)
         smp = make_sample(img, lab, nbrw, sorw)
         if smp is not None and smp.nol <= MAX_SLOTS and min(smp.target.shape[:3]) >= 48:
             out.append(smp)
@@ -353,18 +386,21 @@ def training_set(n, shape=(96, 96, 96), nbrw=10, sorw=4000, seed=0):
 
 
 def _slot_permutation(rng, nol):
-    """Random placement of a sample's nol label slots among the MAX_SLOTS slot
-    channels: (feature channel order, target channel of each slot)."""
-    perm = rng.permutation(MAX_SLOTS)
+    """Random placement of a sample's label slots 1..nol-1 among the slot
+    channels 1..MAX_SLOTS-1: (feature channel order, target channel of each
+    slot). Slot 0 keeps channel 0: it is the walk's answer for voxels that no
+    walk reaches, a rule the network can only learn if it can tell slot 0."""
+    perm = np.concatenate([[0], 1 + rng.permutation(MAX_SLOTS - 1)])
     src = np.arange(IN_CH)
     for k in range(MAX_SLOTS):
         src[3 + perm[k]] = 3 + k
     return src, perm[:nol]
 
 
-def train(net: SurrogateNet, samples, steps, batch=4, patch=96, lr=3e-3, seed=0, log_every=0, permute=True):
+def train(net: SurrogateNet, samples, steps, batch=4, patch=96, lr=2e-3, seed=0, log_every=0, permute=True,
+          warmup=200):
     """AdamW on random windows (patch^3, clipped to the smallest sample) with
-    cosine learning-rate decay. With `permute`, each window's label slots are
+    a linear learning-rate warmup over `warmup` steps and cosine decay. With `permute`, each window's label slots are
     moved to random slot channels (inputs and targets alike), so that the
     network learns the same rule for every slot; the loss then runs over all
     MAX_SLOTS channels. Returns the loss per step."""
@@ -391,18 +427,20 @@ def train(net: SurrogateNet, samples, steps, batch=4, patch=96, lr=3e-3, seed=0,
             feats.append(f)
         xb = torch.cat(feats).contiguous()
         logits = net.forward(xb, keep=True)
-        dls, tot = [], 0.0
+        dls, tot = [], torch.zeros(1, dtype=torch.float32, device=xb.device)
         for k, (t, w, nol) in enumerate(tgts):
-            loss, dl = net.loss_and_grad(logits[k:k + 1].contiguous(), t, w, nol, extra_scale=1.0 / batch)
+            loss, dl = net.loss_and_grad(logits[k:k + 1].contiguous(), t, w, nol, extra_scale=1.0 / batch,
+                                         denom=patch ** 3)
             dls.append(dl)
-            tot += float(loss) / batch
+            tot += loss / batch
         net.zero_grad()
         net.backward(torch.cat(dls).contiguous())
-        net.adamw(lr=lr * 0.5 * (1 + math.cos(math.pi * step / max(steps, 1))))
+        ramp = min(1.0, (step + 1) / warmup) if warmup else 1.0
+        net.adamw(lr=lr * ramp * 0.5 * (1 + math.cos(math.pi * step / max(steps, 1))))
         losses.append(tot)
         if log_every and step % log_every == 0:
-            print(f"step {step}: loss {tot:.4f}", flush=True)
-    return losses
+            print(f"step {step}: loss {float(tot):.4f}", flush=True)
+    return [float(v) for v in losses]
 
 
 def agreement(net: SurrogateNet, smp: Sample) -> dict:
@@ -432,17 +470,35 @@ def load(path, device=None) -> SurrogateNet:
 # ---------------------------------------------------------------------------
 # Hybrid interpolation
 # ---------------------------------------------------------------------------
-def hybrid_interpolation(img, lab, net: SurrogateNet, nbrw=10, sorw=4000, smooth=0, threshold=0.9, radius=48,
-                         coarse=8, rng_seed=None, device_inputs=None):
+def seeds_near(job, mask: torch.Tensor, radius: int, coarse: int = 8) -> torch.Tensor:
+    """Boolean per seed record: the seed lies within about `radius` voxels
+    (Chebyshev distance, rounded up to whole cells of `coarse`^3 voxels) of a
+    voxel set in `mask` ([Zc, Yc, Xc] bool)."""
+    import torch.nn.functional as Fnn
+
+    from .interpolation import SEED_RECORD_BYTES
+
+    cp = job.cplan
+    u = Fnn.max_pool3d(mask[None, None].to(torch.float16), coarse, stride=coarse, ceil_mode=True)
+    r = max(1, int(math.ceil(radius / coarse)))
+    near = Fnn.max_pool3d(u, 2 * r + 1, stride=1, padding=r)[0, 0] > 0
+    n = int(job.n_seeds.item())
+    rec = job.seeds[: n * SEED_RECORD_BYTES].view(torch.int32).view(n, 4)
+    pos = rec[:, 0].to(torch.int64) & 0xFFFFFFFF
+    plane = cp.Yc * cp.Xc
+    return near[pos // plane // coarse, (pos // cp.Xc) % cp.Yc // coarse, pos % cp.Xc // coarse]
+
+
+def hybrid_interpolation(img, lab, net: SurrogateNet, nbrw=10, sorw=4000, smooth=0, threshold=0.97, radius=16,
+                         coarse=4, grow=2, rng_seed=None, device_inputs=None, keep_maps=False):
     """Surrogate probabilities everywhere; the plain walk only from the seeds
     within about `radius` voxels of a voxel whose largest probability is below
-    `threshold` (the uncertain voxels, dilated on a grid of `coarse`^3
-    cells); on the uncertain voxels the walk's hit fractions replace the
+    `threshold`, grown by `grow` voxels (the uncertain voxels; the seed
+    search dilates them on a grid of `coarse`^3 cells); on the uncertain
+    voxels that some walk reached, the walk's hit fractions replace the
     surrogate's probabilities. Labels are the argmax of the combined maps
     (and of their smoothed copy when smooth > 0), remapped like the plain
     method's. Returns (dict of device label volumes, stats)."""
-    import torch.nn.functional as Fnn
-
     from .interpolation import (DEFAULT_RNG_SEED, DeviceJob, SEED_RECORD_BYTES, _IMG_DTYPES, _LAB_DTYPES,
                                 normalize_host_dtypes, upload, walk_sorted)
 
@@ -467,27 +523,27 @@ def hybrid_interpolation(img, lab, net: SurrogateNet, nbrw=10, sorw=4000, smooth
     t1 = time.perf_counter()
     probs = predict(net, job)
     unsure = probs.amax(0) < threshold
+    if grow > 0:
+        import torch.nn.functional as Fnn
+
+        unsure = Fnn.max_pool3d(unsure[None, None].to(torch.float16), 2 * grow + 1, stride=1,
+                                padding=grow)[0, 0] > 0
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    # seeds near uncertain voxels: dilation on a coarse grid
-    u = Fnn.max_pool3d(unsure[None, None].to(torch.float16), coarse, stride=coarse, ceil_mode=True)
-    r = max(1, int(math.ceil(radius / coarse)))
-    near = Fnn.max_pool3d(u, 2 * r + 1, stride=1, padding=r)[0, 0] > 0
-    del u
+    keep = seeds_near(job, unsure, radius, coarse)
     n_seeds = int(job.n_seeds.item())
     rec = job.seeds[: n_seeds * SEED_RECORD_BYTES].view(torch.int32).view(n_seeds, 4)
-    pos = rec[:, 0].to(torch.int64) & 0xFFFFFFFF
-    plane = cp.Yc * cp.Xc
-    keep = near[pos // plane // coarse, (pos // cp.Xc) % cp.Yc // coarse, pos % cp.Xc // coarse]
-    del pos
     kept = rec[keep].contiguous()
     n_keep = int(kept.shape[0])
     hits = torch.zeros((nol, cp.Zc, cp.Yc, cp.Xc), dtype=torch.int32, device=job.dev)
     sweeps = 0
+    ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    ev[0].record()
     if n_keep:
         cnt = torch.tensor([n_keep], dtype=torch.int32, device=job.dev)
         sweeps = walk_sorted(job.packed, False, cp.Zc, cp.Yc, cp.Xc, kept.view(torch.uint8).reshape(-1), cnt, n_keep,
                              nbrw, sorw, job.rng_seed, hits, nol)
+    ev[1].record()
     del kept
     torch.cuda.synchronize()
     t3 = time.perf_counter()
@@ -511,7 +567,9 @@ def hybrid_interpolation(img, lab, net: SurrogateNet, nbrw=10, sorw=4000, smooth
              "seconds_post": t4 - t3, "seconds_total": t4 - t0, "frac_uncertain": float(unsure.float().mean()),
              "frac_walked_voxels": float(use.float().mean()), "seeds_walked": n_keep, "seeds_total": n_seeds,
              "frac_seeds_walked": n_keep / max(n_seeds, 1), "walker_steps": n_keep * nbrw * sorw,
-             "sweeps": sweeps, "nol": nol}
+             "sweeps": sweeps, "nol": nol, "walk_ms_events": ev[0].elapsed_time(ev[1])}
+    if keep_maps:
+        res["use"] = use
     return res, stats
 
 

@@ -288,10 +288,15 @@ int si_nn_conv3d_fwd(const void* x, const void* w, const float* bias,
                      void* stream);
 
 /* dw[27][cout][cin] += sum_v dy[v][co] x[v + off][ci]; db[cout] += sum_v dy
- * (db nullable). (cout, cin) in {16, 32}^2. */
+ * (db nullable). (cout, cin) in {16, 32}^2. With `partials` (cin = cout = 16
+ * only; size from si_nn_wgrad_partial_bytes, 16-byte aligned) every block
+ * writes its own sums and a second pass adds them in block order, so the
+ * result is deterministic; with partials = NULL blocks add with atomics. */
+int si_nn_wgrad_partial_bytes(int N, int D, int H, int W, int cin, int cout,
+                              uint64_t* bytes);
 int si_nn_conv3d_wgrad(const void* x, const void* dy, float* dw, float* db,
                        int N, int D, int H, int W, int cin, int cout, int dil,
-                       void* stream);
+                       float* partials, uint64_t partial_bytes, void* stream);
 
 /* w_flipped[tap][ci][co] = w[26 - tap][co][ci] (data-gradient weights). */
 int si_nn_flip_weights(const void* w, void* w_flipped, int cout, int cin,
