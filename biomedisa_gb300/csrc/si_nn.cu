@@ -456,13 +456,18 @@ __global__ void __launch_bounds__(256) bias_grad_kernel(const __nv_bfloat16* __r
   }
 }
 
-// out[i] += sum_b partials[b][i], b ascending (n outputs, nb blocks)
+// out[i] += sum_b partials[b][i] (n outputs, nb blocks). One warp per
+// output: lane l sums b = l, l + 32, ... in order, then a fixed shuffle tree
+// combines the lanes, so the result does not depend on scheduling.
 __global__ void __launch_bounds__(256) reduce_partials_kernel(const float* __restrict__ partials, int nb, int n,
                                                               float* __restrict__ out) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
     float s = 0.0f;
-    for (int b = 0; b < nb; ++b) s += partials[(int64_t)b * n + i];
-    out[i] += s;
+    for (int b = lane; b < nb; b += 32) s += partials[(int64_t)b * n + i];
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[i] += s;
   }
 }
 
@@ -703,7 +708,7 @@ extern "C" int si_nn_conv3d_wgrad(const void* x, const void* dy, float* dw, floa
     const int64_t blocks = (rows + per - 1) / per;
     wgrad16_kernel<<<(unsigned)blocks, 128, 0, st>>>(xb, db16, dw, partials, g, dil, xchunks, per);
     if (partials)
-      reduce_partials_kernel<<<(27 * 256 + 255) / 256, 256, 0, st>>>(partials, (int)blocks, 27 * 256, dw);
+      reduce_partials_kernel<<<27 * 256 / 8, 256, 0, st>>>(partials, (int)blocks, 27 * 256, dw);
   } else if (cout == 16 && cin == 16) conv3d_wgrad_kernel<16, 16><<<grid, 128, 0, st>>>(xb, db16, dw, g, dil);
   else if (cout == 32 && cin == 16) conv3d_wgrad_kernel<32, 16><<<grid, 128, 0, st>>>(xb, db16, dw, g, dil);
   else if (cout == 16 && cin == 32) conv3d_wgrad_kernel<16, 32><<<grid, 128, 0, st>>>(xb, db16, dw, g, dil);
@@ -714,7 +719,7 @@ extern "C" int si_nn_conv3d_wgrad(const void* x, const void* dy, float* dw, floa
     float* bpart = partials ? partials + (int64_t)sm_count() * 8 * 27 * cout * cin : nullptr;
     if (cout == 16) bias_grad_kernel<16><<<bb, 256, 0, st>>>(db16, V, db, bpart);
     else bias_grad_kernel<32><<<bb, 256, 0, st>>>(db16, V, db, bpart);
-    if (bpart) reduce_partials_kernel<<<1, 256, 0, st>>>(bpart, bb, cout, db);
+    if (bpart) reduce_partials_kernel<<<(cout + 7) / 8, 256, 0, st>>>(bpart, bb, cout, db);
   }
   return check_launch("si_nn_conv3d_wgrad");
 }
