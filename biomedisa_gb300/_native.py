@@ -64,6 +64,10 @@ _SIGNATURES = {
     "si_nn_features": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int,
                        _c_int, _c_int, _c_void_p, _c_void_p],
     "si_nn_probs": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_int, _c_int, _c_void_p],
+    "si_cc_scratch_bytes": [_c_int, _c_int, _c_int, _c_void_p],
+    "si_clean": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, ctypes.c_double, _c_int, _c_void_p, _c_u64,
+                 _c_void_p],
+    "si_fill": [_c_void_p, _c_int, _c_int, _c_int, ctypes.c_double, _c_void_p, _c_int, _c_void_p, _c_u64, _c_void_p],
     "si_smooth_f32": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
     "si_smooth": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
 }

@@ -13,8 +13,8 @@ libsmartinterp.so on one GPU. Differences from the reference, by design:
     reference's literal 0.01 is binary64);
   * every volume takes the plain full walk (the reference switches to its
     seed-subsampling large path above 2e9 bytes, interpolation.py:196);
-  * file I/O, MPI ranks, Django and post-processing (clean/fill/acwe) are not
-    part of this path.
+  * file I/O, MPI ranks, Django and acwe are not part of this path; clean and
+    fill run on the device (postprocess.py).
 """
 from __future__ import annotations
 
@@ -453,7 +453,9 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
 
     Same parameters and result keys as the reference
     (biomedisa/interpolation.py:43-46; results 'regular' and, when asked,
-    'smooth', 'uncertainty', 'hits'). Errors print 'Error: ...' and return
+    'smooth', 'uncertainty', 'hits', and with ``clean`` / ``fill`` thresholds
+    'cleaned', 'smooth_cleaned', 'filled', 'cleaned_filled' as
+    rw_small.py:223-243). Errors print 'Error: ...' and return
     None as the reference does. ``platform`` is accepted and ignored (one CUDA
     device). Extra keyword-only arguments: ``rng_seed`` (Philox key),
     ``device``, ``return_device`` (keep results as device tensors), ``walker``
@@ -465,8 +467,8 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
     """
     if data is None or labelData is None:
         raise NotImplementedError("loading volumes from files is outside this package; pass numpy arrays")
-    if acwe or clean is not None or fill is not None:
-        raise NotImplementedError("acwe/clean/fill post-processing is not implemented on this path")
+    if acwe:
+        raise NotImplementedError("acwe post-processing is not implemented on this path")
     if not torch.cuda.is_available():
         raise RuntimeError("smart_interpolation needs a CUDA device; there is no CPU fallback")
     data = np.asarray(data)
@@ -487,6 +489,10 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
     job.prepare()
     job.walk()
     res = job.post(return_hits=return_hits)
+    if clean or fill:
+        from .postprocess import post_results
+
+        post_results(res, clean, fill)
     # sanity check of rw_small.py:203-211 (Dice of the input slices vs result)
     mask = lab > 0
     gt = lab.to(torch.int32)

@@ -275,6 +275,31 @@ int si_smooth(uint32_t* maps, float* tmp0, float* tmp1, int nol, int Zc,
 int si_smooth_f32(float* maps, float* tmp0, float* tmp1, int nol, int Zc,
                   int Yc, int Xc, int iters, void* stream);
 
+/* ---- outlier removal and hole filling (remove_outlier.py:67-141) ----
+ * uint8 label volumes (Z, Y, X), at most 2^31 - 1 voxels; 6-connected
+ * components by union-find. Scratch: si_cc_scratch_bytes (16-byte aligned). */
+int si_cc_scratch_bytes(int Z, int Y, int X, uint64_t* bytes);
+
+/* clean (remove_outlier.py:67-105): out = labels, except that voxels of a
+ * 6-connected component of a label whose size is not > threshold x the
+ * label's largest component become 0. Voxels of skip_label (the smallest
+ * label present; -1 for none) are left alone. Replaces remove_outlier.clean. */
+int si_clean(const uint8_t* labels, uint8_t* out, int Z, int Y, int X,
+             double threshold, int skip_label, void* scratch,
+             uint64_t scratch_bytes, void* stream);
+
+/* fill (remove_outlier.py:107-141), in place, for the labels of label_list
+ * in that order (host array; the reference's labels after the smallest):
+ * inside each label's bounding box grown by one voxel, the complement's
+ * 6-connected components (box-confined) are filled with the label unless
+ * the component is the first maximum of [label size, component sizes] or
+ * larger than threshold x label size; if the label itself is that maximum,
+ * its voxels become 0. A label with no voxels left is skipped (the reference
+ * raises there). Replaces remove_outlier.fill. */
+int si_fill(uint8_t* img, int Z, int Y, int X, double threshold,
+            const int* label_list, int n_labels, void* scratch,
+            uint64_t scratch_bytes, void* stream);
+
 /* ---- learned surrogate (no counterpart in the reference) ----
  * Tensors are NDHWC; activations bfloat16, weights bfloat16 [27][cout][cin]
  * (tap-major, tap = (dz+1)*9 + (dy+1)*3 + (dx+1)), biases and gradients fp32.

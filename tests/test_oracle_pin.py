@@ -126,3 +126,30 @@ def test_oracle_reference_mode_matches_reference_kernels_live(seed):
                             st.ctypes.data_as(ctypes.c_void_p), a.ctypes.data_as(ctypes.c_void_p), X, Y, Z,
                             ind.ctypes.data_as(ctypes.c_void_p), 45, 2)
         assert np.array_equal(a, hits[s].astype(np.float32)), f"label {seg}"
+
+
+def test_cc_oracle_matches_reference_clean_fill():
+    """oracle/cc_oracle.py against the reference's own clean() and fill()
+    (tests/golden/ref_cc.npz, made by tests/golden/make_golden_cc.py)."""
+    import cc_oracle as C
+    z = np.load(GOLDEN / "ref_cc.npz")
+    names = sorted(k[:-3] for k in z.files if k.endswith("_in"))
+    assert len(names) >= 6
+    for n in names:
+        v = z[f"{n}_in"]
+        for thr in (0.1, 0.5):
+            assert np.array_equal(C.clean(v, thr), z[f"{n}_clean_{thr}"]), (n, thr)
+        for thr in (0.9, 0.3):
+            assert np.array_equal(C.fill(v, thr), z[f"{n}_fill_{thr}"]), (n, thr)
+
+
+def test_cc_oracle_skips_vanished_label():
+    """A label covered entirely by an earlier label's filling is skipped (the
+    reference raises on the empty box)."""
+    import cc_oracle as C
+    v = np.zeros((12, 12, 12), np.uint8)
+    v[2:10, 2:10, 2:10] = 1
+    v[4:8, 4:8, 4:8] = 0
+    v[5:7, 5:7, 5:7] = 2
+    out = C.fill(v, 0.9)
+    assert (out[2:10, 2:10, 2:10] == 1).all() and not (out == 2).any()
