@@ -32,6 +32,13 @@ _SIGNATURES = {
     "si_extract_seeds_noalloc": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int,
                                  _c_int, _c_void_p, _c_void_p, _c_void_p, _c_int, _c_void_p, _c_int, _c_void_p,
                                  _c_void_p, _c_void_p],
+    "si_extract_seeds_box": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int,
+                             _c_int, _c_void_p, _c_void_p, _c_void_p, _c_int, _c_void_p, _c_int, _c_int, _c_int,
+                             _c_int, _c_int, _c_void_p, _c_void_p, _c_void_p, _c_void_p],
+    "si_adaptive_scratch_bytes": [_c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_adaptive_seed_filter": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int,
+                                _c_int, _c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int,
+                                _c_void_p, _c_void_p, _c_u32, _c_void_p, _c_void_p, _c_void_p, _c_u64, _c_void_p],
     "si_pack_neighbours": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_void_p],
     "si_walk": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_void_p, _c_u32, _c_int, _c_int, _c_u64,
                 _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p],

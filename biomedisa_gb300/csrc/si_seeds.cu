@@ -19,6 +19,7 @@ struct SeedGeom {
   int cz0, cy0, cx0;
   int Zc, Yc, Xc;
   int max_rows;
+  int by0, by1, bx0, bx1;  // in-plane box (crop y, x); labels outside read as ignored (-1)
 };
 
 __device__ __forceinline__ int rows_of(const SeedGeom& g, int axis) { return axis == 0 ? g.Yc : g.Zc; }
@@ -42,6 +43,7 @@ struct SlotView {
   SeedGeom g;
   // label slot at crop coordinates; -1 = no slot (negative label).
   __device__ __forceinline__ int slot(int z, int y, int x) const {
+    if (y < g.by0 || y >= g.by1 || x < g.bx0 || x >= g.bx1) return -1;
     const int oz = z + g.cz0 - 1, oy = y + g.cy0 - 1, ox = x + g.cx0 - 1;
     int v = 0;  // pad voxels carry label 0
     if ((unsigned)oz < (unsigned)g.Z0 && (unsigned)oy < (unsigned)g.Y0 && (unsigned)ox < (unsigned)g.X0)
@@ -221,11 +223,11 @@ __global__ void __launch_bounds__(128) seed_emit_kernel(const T* __restrict__ la
 
 using namespace si;
 
-extern "C" int si_extract_seeds(const void* labels, int dtype, int Z0, int Y0, int X0, int cz0, int cy0, int cx0,
-                                int Zc, int Yc, int Xc, const int16_t* slot_lut, const uint8_t* slot_label,
-                                const void* work, int work_is_float, const int32_t* slice_list, int n_slices,
-                                uint32_t* row_counts, si_seed_t* seeds, uint32_t* n_seeds, void* stream) {
-  clear_error();
+static int extract_seeds_impl(const void* labels, int dtype, int Z0, int Y0, int X0, int cz0, int cy0, int cx0,
+                              int Zc, int Yc, int Xc, const int16_t* slot_lut, const uint8_t* slot_label,
+                              const void* work, int work_is_float, const int32_t* slice_list, int n_slices,
+                              uint32_t* row_counts, si_seed_t* seeds, uint32_t* n_seeds, int by0, int by1, int bx0,
+                              int bx1, void* stream) {
   if (!labels || !slot_lut || !slot_label || !work || !row_counts || !seeds || !n_seeds)
     return set_error(SI_ERR_ARG, "si_extract_seeds: null pointer");
   if (n_slices < 0 || (n_slices > 0 && !slice_list)) return set_error(SI_ERR_ARG, "si_extract_seeds: bad slice list");
@@ -239,7 +241,7 @@ extern "C" int si_extract_seeds(const void* labels, int dtype, int Z0, int Y0, i
       return set_error(SI_ERR_CUDA, "si_extract_seeds: memset failed");
     return SI_OK;
   }
-  SeedGeom g{Z0, Y0, X0, cz0, cy0, cx0, Zc, Yc, Xc, Zc > Yc ? Zc : Yc};
+  SeedGeom g{Z0, Y0, X0, cz0, cy0, cx0, Zc, Yc, Xc, Zc > Yc ? Zc : Yc, by0, by1, bx0, bx1};
   const dim3 grid(g.max_rows, n_slices);
   const uint32_t n = (uint32_t)((size_t)n_slices * g.max_rows);
   SeedRec* out = reinterpret_cast<SeedRec*>(seeds);
@@ -270,6 +272,27 @@ extern "C" int si_extract_seeds(const void* labels, int dtype, int Z0, int Y0, i
   }
 #undef SI_SEEDS_FOR
   return check_launch("si_extract_seeds");
+}
+
+extern "C" int si_extract_seeds(const void* labels, int dtype, int Z0, int Y0, int X0, int cz0, int cy0, int cx0,
+                                int Zc, int Yc, int Xc, const int16_t* slot_lut, const uint8_t* slot_label,
+                                const void* work, int work_is_float, const int32_t* slice_list, int n_slices,
+                                uint32_t* row_counts, si_seed_t* seeds, uint32_t* n_seeds, void* stream) {
+  clear_error();
+  return extract_seeds_impl(labels, dtype, Z0, Y0, X0, cz0, cy0, cx0, Zc, Yc, Xc, slot_lut, slot_label, work,
+                            work_is_float, slice_list, n_slices, row_counts, seeds, n_seeds, 0, Yc, 0, Xc, stream);
+}
+
+extern "C" int si_extract_seeds_box(const void* labels, int dtype, int Z0, int Y0, int X0, int cz0, int cy0,
+                                    int cx0, int Zc, int Yc, int Xc, const int16_t* slot_lut,
+                                    const uint8_t* slot_label, const void* work, int work_is_float,
+                                    const int32_t* slice_list, int n_slices, int box_y0, int box_y1, int box_x0,
+                                    int box_x1, uint32_t* row_counts, si_seed_t* seeds, uint32_t* n_seeds,
+                                    void* stream) {
+  clear_error();
+  return extract_seeds_impl(labels, dtype, Z0, Y0, X0, cz0, cy0, cx0, Zc, Yc, Xc, slot_lut, slot_label, work,
+                            work_is_float, slice_list, n_slices, row_counts, seeds, n_seeds, box_y0, box_y1, box_x0,
+                            box_x1, stream);
 }
 
 // ---------------------------------------------------------------------------

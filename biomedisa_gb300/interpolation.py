@@ -29,6 +29,7 @@ from . import _native as nat
 
 DEFAULT_RNG_SEED = 0x243F6A8885A308D3
 WALKERS = ("auto", "sorted", "tiles", "packed")
+SEEDINGS = ("plain", "large")
 SEED_RECORD_BYTES = 16
 
 
@@ -212,9 +213,14 @@ class DeviceJob:
     def __init__(self, img: torch.Tensor, img_code: int, lab: torch.Tensor, lab_code: int, *, nbrw=10, sorw=4000,
                  allaxis=False, smooth=0, uncertainty=False, denoise=False, only="all", ignore="none",
                  rng_seed=DEFAULT_RNG_SEED, walk_grid=0, walk_block=0, walk_order=0, walker="auto",
-                 sweep_steps=0, sort_edge=0):
+                 sweep_steps=0, sort_edge=0, seeding="plain"):
         if walker not in WALKERS:
             raise ValueError(f"walker must be one of {WALKERS}")
+        if seeding not in SEEDINGS:
+            raise ValueError(f"seeding must be one of {SEEDINGS}")
+        if seeding == "large" and allaxis:
+            raise ValueError("large-path seeding is supported for z-slices only (allaxis=False)")
+        self.seeding = seeding
         self.sweep_steps = int(sweep_steps)
         self.sort_edge = int(sort_edge)
         self.walker = walker
@@ -289,18 +295,24 @@ class DeviceJob:
         self.seed_capacity = cap
         self.seeds = torch.empty(cap * SEED_RECORD_BYTES, dtype=torch.uint8, device=self.dev)
         self.n_seeds = torch.zeros(1, dtype=torch.int32, device=self.dev)
-        n_sl = len(cp.slice_list)
+        slice_list = cp.slice_list
+        if self.seeding == "large":
+            slice_list = large_slice_list(cp.slice_list)
+        n_sl = len(slice_list)
         self.row_counts = torch.zeros(max(n_sl * cp.max_rows + 1, 1), dtype=torch.int32, device=self.dev)
-        sl = torch.from_numpy(np.ascontiguousarray(cp.slice_list.reshape(-1))).to(self.dev) if n_sl else \
+        sl = torch.from_numpy(np.ascontiguousarray(slice_list.reshape(-1))).to(self.dev) if n_sl else \
             torch.zeros(2, dtype=torch.int32, device=self.dev)
         slot_lut = torch.from_numpy(self.lplan.slot_lut).to(self.dev)
         slot_label = np.zeros(256, np.uint8)
         slot_label[: self.lplan.nol] = self.lplan.all_labels.astype(np.uint8)
         self.slot_label = torch.from_numpy(slot_label).to(self.dev)
-        nat.call("si_extract_seeds", _ptr(self.lab), self.lab_code, *self.shape0, *cp.crop, _ptr(slot_lut),
-                 _ptr(self.slot_label), _ptr(self.work), int(self.work_is_float), _ptr(sl), n_sl,
-                 _ptr(self.row_counts), _ptr(self.seeds), _ptr(self.n_seeds), _stream())
-        self.launches += 3
+        if self.seeding == "large":
+            self._large_seeds(slice_list, sl, slot_lut)
+        else:
+            nat.call("si_extract_seeds", _ptr(self.lab), self.lab_code, *self.shape0, *cp.crop, _ptr(slot_lut),
+                     _ptr(self.slot_label), _ptr(self.work), int(self.work_is_float), _ptr(sl), n_sl,
+                     _ptr(self.row_counts), _ptr(self.seeds), _ptr(self.n_seeds), _stream())
+            self.launches += 3
         long_walks = self.nbrw * self.sorw >= (1 << 24)
         kind = self.walker
         if kind == "auto":
@@ -313,6 +325,28 @@ class DeviceJob:
         if kind != "tiles":
             self.packed = pack_neighbours(self.work, self.work_is_float, cp.Zc, cp.Yc, cp.Xc)
             self.launches += 1
+
+    def _large_seeds(self, slice_list, sl, slot_lut):
+        """The reference large path's seed set: taken slices (slice_list),
+        labels outside the in-plane box read as ignored, adaptive filter."""
+        cp = self.cplan
+        taken = [int(z) for _, z in slice_list.tolist()]
+        self.large_box = large_slice_box(self, taken)
+        y0, y1, x0, x1 = self.large_box
+        n_sl = len(taken)
+        raw = torch.empty_like(self.seeds)
+        n_raw = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        nat.call("si_extract_seeds_box", _ptr(self.lab), self.lab_code, *self.shape0, *cp.crop, _ptr(slot_lut),
+                 _ptr(self.slot_label), _ptr(self.work), int(self.work_is_float), _ptr(sl), n_sl, y0, y1, x0, x1,
+                 _ptr(self.row_counts), _ptr(raw), _ptr(n_raw), _stream())
+        need = ctypes.c_uint64(0)
+        nat.call("si_adaptive_scratch_bytes", cp.Zc, cp.Yc, cp.Xc, n_sl, ctypes.byref(need))
+        scratch = torch.empty(max(int(need.value), 1), dtype=torch.uint8, device=self.dev)
+        zs = torch.tensor(taken if taken else [0], dtype=torch.int32, device=self.dev)
+        nat.call("si_adaptive_seed_filter", _ptr(self.lab), self.lab_code, *self.shape0, *cp.crop, _ptr(slot_lut),
+                 _ptr(self.slot_label), _ptr(zs), n_sl, y0, y1, x0, x1, _ptr(raw), _ptr(n_raw), self.seed_capacity,
+                 _ptr(self.seeds), _ptr(self.n_seeds), _ptr(scratch), int(need.value), _stream())
+        self.launches += 3 + 5
 
     def walk(self):
         cp = self.cplan
@@ -375,6 +409,10 @@ class DeviceJob:
         self.launches += self.lplan.nol * max(self.smooth, 1)
 
     def post_smooth(self):
+        if self.seeding == "large":
+            # pycuda_large.py:440-444: label 0's smoothed map is clamped at 0
+            plane = self.hits[0].view(torch.float32)
+            plane.clamp_(min=0.0)
         sm, _ = self._labels_from(self.hits, True, False)
         return sm
 
@@ -392,6 +430,55 @@ class DeviceJob:
 
     def total_steps(self) -> int:
         return int(self.n_seeds.item()) * self.nbrw * self.sorw
+
+
+def large_slice_list(slice_list: np.ndarray) -> np.ndarray:
+    """read_labeled_slices_large (biomedisa_helper.py:1068-1080) on the crop's
+    labelled z-slices: after each slice taken, the next four are skipped."""
+    out, nxt = [], -1
+    for axis, z in slice_list.tolist():
+        if axis == 0 and z >= nxt:
+            out.append((0, z))
+            nxt = z + 5
+    return np.asarray(out, np.int32).reshape(-1, 2)
+
+
+def large_slice_box(job, taken) -> tuple[int, int, int, int]:
+    """reduceBlocksize (pycuda_large.py:39-58) on the taken slices of the
+    crop: box of the non-zero labels of the slices whose non-zero voxels are
+    not all in crop column 0, grown by 100 voxels and clamped; (y0, y1, x0,
+    x1) in crop coordinates, labels outside read as -1."""
+    cp = job.cplan
+    Z0, Y0, X0 = job.shape0
+    Yc, Xc = cp.Yc, cp.Xc
+    amin_x, amax_x, amin_y, amax_y = Xc, 0, Yc, 0
+    if taken:
+        oy, ox = cp.cy0 - 1, cp.cx0 - 1
+        ys, ye, xs, xe = max(oy, 0), min(oy + Yc, Y0), max(ox, 0), min(ox + Xc, X0)
+        oz = torch.tensor([z + cp.cz0 - 1 for z in taken], dtype=torch.int64, device=job.dev)
+        v = job.lab.index_select(0, oz)[:, ys:ye, xs:xe].to(torch.int32)
+        eff_lut = np.zeros(256, np.int32)
+        for k in range(256):
+            slot = int(job.lplan.slot_lut[k])
+            eff_lut[k] = int(job.lplan.all_labels[slot]) if slot >= 0 else 0
+        lut = torch.from_numpy(eff_lut).to(job.dev)
+        eff = torch.where(v < 0, v, torch.where(v > 255, torch.zeros_like(v), lut[v.clamp(0, 255).long()]))
+        nz = eff != 0
+        xcoord = torch.arange(xs - ox, xe - ox, device=job.dev)  # crop columns of the loaded ones
+        qual = (nz & (xcoord != 0)[None, None, :]).flatten(1).any(1)
+        nzq = nz & qual[:, None, None]
+        rows = nzq.any(2).any(0)
+        cols = nzq.any(1).any(0)
+        if bool(rows.any()):
+            ry = torch.nonzero(rows).flatten()
+            cx = torch.nonzero(cols).flatten()
+            amin_y, amax_y = int(ry[0]) + ys - oy, int(ry[-1]) + ys - oy
+            amin_x, amax_x = int(cx[0]) + xs - ox, int(cx[-1]) + xs - ox
+    amin_x = amin_x - 100 if amin_x - 100 > 0 else 0
+    amax_x = amax_x + 100 if amax_x + 100 < Xc else Xc
+    amin_y = amin_y - 100 if amin_y - 100 > 0 else 0
+    amax_y = amax_y + 100 if amax_y + 100 < Yc else Yc
+    return amin_y, amax_y, amin_x, amax_x
 
 
 def pack_neighbours(work: torch.Tensor, is_float: bool, Zc: int, Yc: int, Xc: int) -> torch.Tensor:
@@ -448,7 +535,8 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
                         platform=None, allaxis=False, ignore="none", only="all", smooth=0, compression=True,
                         return_hits=False, img_id=None, label_id=None, remote=False, queue=0, clean=None, fill=None,
                         slicer=False, *, rng_seed=DEFAULT_RNG_SEED, device=None, return_device=False,
-                        walk_grid=0, walk_block=0, walk_order=0, walker="auto", sweep_steps=0, sort_edge=0):
+                        walk_grid=0, walk_block=0, walk_order=0, walker="auto", sweep_steps=0, sort_edge=0,
+                        seeding="plain"):
     """Smart interpolation of sparsely pre-segmented slices on one GB300.
 
     Same parameters and result keys as the reference
@@ -463,7 +551,9 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
     ``sort_edge``^3 voxels (0 = library defaults); 'tiles':
     shared-memory brick walker, uint8 only; 'packed': one thread per walk) and
     the packed walker's launch shape (``walk_grid``, ``walk_block``,
-    ``walk_order``). All walkers give identical hit maps.
+    ``walk_order``). All walkers give identical hit maps. ``seeding='large'``
+    walks the seed set of the reference's large path (slice skipping, label
+    box, adaptive seeds; z-slices only) instead of every seed.
     """
     if data is None or labelData is None:
         raise NotImplementedError("loading volumes from files is outside this package; pass numpy arrays")
@@ -482,7 +572,8 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
     job = DeviceJob(img, _IMG_DTYPES[np.dtype(data.dtype)], lab, _LAB_DTYPES[np.dtype(labelData.dtype)], nbrw=nbrw,
                     sorw=sorw, allaxis=allaxis, smooth=smooth, uncertainty=uncertainty, denoise=denoise, only=only,
                     ignore=ignore, rng_seed=rng_seed, walk_grid=walk_grid, walk_block=walk_block,
-                    walk_order=walk_order, walker=walker, sweep_steps=sweep_steps, sort_edge=sort_edge)
+                    walk_order=walk_order, walker=walker, sweep_steps=sweep_steps, sort_edge=sort_edge,
+                    seeding=seeding)
     msg = job.analyze()
     if msg:
         return _err(msg)

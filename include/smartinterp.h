@@ -275,6 +275,39 @@ int si_smooth(uint32_t* maps, float* tmp0, float* tmp1, int nol, int Zc,
 int si_smooth_f32(float* maps, float* tmp0, float* tmp1, int nol, int Zc,
                   int Yc, int Xc, int iters, void* stream);
 
+/* ---- the reference large path's seed set (optional mode) ----
+ * si_extract_seeds with an in-plane box [box_y0, box_y1) x [box_x0, box_x1)
+ * (crop y, x) outside which labels read as ignored (-1), as the large path's
+ * slice stack after reduceBlocksize (pycuda_large.py:39-58): no seeds there
+ * and no contribution to the neighbours' 3x3 variance. */
+int si_extract_seeds_box(const void* labels, int dtype, int Z0, int Y0, int X0,
+                         int cz0, int cy0, int cx0, int Zc, int Yc, int Xc,
+                         const int16_t* slot_lut, const uint8_t* slot_label,
+                         const void* work, int work_is_float,
+                         const int32_t* slice_list, int n_slices, int box_y0,
+                         int box_y1, int box_x0, int box_x1,
+                         uint32_t* row_counts, si_seed_t* seeds,
+                         uint32_t* n_seeds, void* stream);
+
+/* Adaptive seeds (pycuda_large.py:513-533): copies to seeds_out (count in
+ * *n_out) the z-slice seeds of seeds_in (*n_in of at most max_in) with
+ * (row + column) % 4 == 0 or a label other than their own and -1 within the
+ * in-slice window [-100, 100]^2 clipped to the crop interior. slice_z: crop z
+ * of the n_slices taken slices (device). Output order is not the input
+ * order. Scratch: si_adaptive_scratch_bytes (256-byte aligned). */
+int si_adaptive_scratch_bytes(int Zc, int Yc, int Xc, int n_slices,
+                              uint64_t* bytes);
+int si_adaptive_seed_filter(const void* labels, int dtype, int Z0, int Y0,
+                            int X0, int cz0, int cy0, int cx0, int Zc, int Yc,
+                            int Xc, const int16_t* slot_lut,
+                            const uint8_t* slot_label, const int32_t* slice_z,
+                            int n_slices, int box_y0, int box_y1, int box_x0,
+                            int box_x1, const si_seed_t* seeds_in,
+                            const uint32_t* n_in, uint32_t max_in,
+                            si_seed_t* seeds_out, uint32_t* n_out,
+                            void* scratch, uint64_t scratch_bytes,
+                            void* stream);
+
 /* ---- outlier removal and hole filling (remove_outlier.py:67-141) ----
  * uint8 label volumes (Z, Y, X), at most 2^31 - 1 voxels; 6-connected
  * components by union-find. Scratch: si_cc_scratch_bytes (16-byte aligned). */

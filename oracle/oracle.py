@@ -337,6 +337,80 @@ class Seeds:
         return weight_constant(self.var)
 
 
+def read_labeled_slices_large(arr):
+    """biomedisa_helper.py:1068-1080: z-slices with any non-zero label; after
+    each one taken, the next four are skipped."""
+    idx, i = [], 0
+    while i < arr.shape[0]:
+        if np.any(arr[i]):
+            idx.append(i)
+            i += 5
+        else:
+            i += 1
+    return idx
+
+
+def large_slice_box(stack):
+    """pycuda_large.py:39-58 (reduceBlocksize) on the stack of taken slices:
+    the in-plane box of the non-zero labels of slices whose non-zero voxels
+    are not all in column 0, grown by 100 and clamped; returns (y0, y1, x0,
+    x1) — the stack is -1 outside [y0, y1) x [x0, x1)."""
+    zsh, ysh, xsh = stack.shape
+    amin_x, amax_x, amin_y, amax_y = xsh, 0, ysh, 0
+    for k in range(zsh):
+        y, x = np.nonzero(stack[k])
+        if x.any():
+            amin_x = min(amin_x, int(np.amin(x)))
+            amax_x = max(amax_x, int(np.amax(x)))
+            amin_y = min(amin_y, int(np.amin(y)))
+            amax_y = max(amax_y, int(np.amax(y)))
+    amin_x = amin_x - 100 if amin_x - 100 > 0 else 0
+    amax_x = amax_x + 100 if amax_x + 100 < xsh else xsh
+    amin_y = amin_y - 100 if amin_y - 100 > 0 else 0
+    amax_y = amax_y + 100 if amax_y + 100 < ysh else ysh
+    return amin_y, amax_y, amin_x, amax_x
+
+
+def large_labels(work_labels, idx):
+    """The cropped label volume as the large walker sees it: the taken
+    z-slices with -1 outside their box (for seeds and their variance)."""
+    lab = np.array(work_labels, dtype=np.int32, copy=True)
+    if not idx:
+        return lab, None
+    stack = lab[idx]
+    y0, y1, x0, x1 = large_slice_box(stack)
+    stack[:, :y0] = -1
+    stack[:, y1:] = -1
+    stack[:, :, :x0] = -1
+    stack[:, :, x1:] = -1
+    lab[idx] = stack
+    return lab, (y0, y1, x0, x1)
+
+
+def adaptive_seed_mask(large_lab, seeds):
+    """pycuda_large.py:513-533 (adaptive random walks): a z-slice seed walks
+    iff (row + column) % 4 == 0 or its in-slice window [-100, 100]^2, clipped
+    to the interior rows/columns 1..n-2, holds a label that is neither its own
+    nor -1. Rows/columns are crop coordinates; large_lab from large_labels."""
+    Z, Y, X = large_lab.shape
+    keep = np.zeros(len(seeds), bool)
+    for i in range(len(seeds)):
+        p = int(seeds.pos[i])
+        z, y, x = p // (Y * X), (p // X) % Y, p % X
+        if (y + x) % 4 == 0:
+            keep[i] = True
+            continue
+        w = large_lab[z, max(1, y - 100):min(Y - 1, y + 101), max(1, x - 100):min(X - 1, x + 101)]
+        own = int(seeds.label[i])
+        keep[i] = bool(np.any((w != own) & (w != -1)))
+    return keep
+
+
+def subset_seeds(seeds, mask):
+    return Seeds(**{f: getattr(seeds, f)[mask] for f in
+                    ("pos", "slot", "axis", "label", "b", "var", "rng_cuda", "rng_ocl")})
+
+
 def _slice_view(vol, axis, s):
     """2-D slice (rows, cols) of a working volume for a seed axis, in the
     row/column convention of the swapped arrays of interpolation.py:212-220."""
@@ -642,14 +716,17 @@ def uncertainty(maps):
 
 def smart_interpolation(data, labelData, nbrw=10, sorw=4000, smooth_iters=0, allaxis=False, uncertainty_map=False,
                         return_hits=False, denoise=False, only="all", ignore="none", key=0, walker="c",
-                        smooth_update="f32", mode="philox"):
+                        smooth_update="f32", mode="philox", seeding="plain"):
     """The reference's small path with the oracle walk.
 
     mode 'philox': the product's semantics (Philox stream, exp2 weights,
     binary32 smoothing update). mode 'reference': the reference's own
     randomness and arithmetic (binary32 MRG stream seeded per seed as the CUDA
     walker does, expf weights, binary64 smoothing update) — used to pin this
-    restatement against the reference's outputs."""
+    restatement against the reference's outputs. seeding 'large': the
+    reference large path's seed set (slice skipping, in-plane label box,
+    adaptive seeds; biomedisa_helper.py:1068-1080, pycuda_large.py:39-58 and
+    :513-533) with the same walk."""
     if mode == "reference":
         smooth_update = "ref_f64"
     labelData, allLabels = pre_processing(labelData, only, ignore)
@@ -673,9 +750,18 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, smooth_iters=0, all
         t2 = np.ascontiguousarray(np.swapaxes(t1, 0, 2))
         sl += [(k, 2) for (k, _) in read_indices_allx(t2, 2)]
         slice_list = [(a, k) for (k, a) in sl]
+    elif seeding == "large":
+        slice_list = [(0, k) for k in read_labeled_slices_large(lab)]
     else:
         slice_list = [(0, k) for k in read_labeled_slices(lab)[0]]
-    seeds = extract_seeds(data, lab, slice_list, allLabels)
+    if seeding == "large":
+        if allaxis:
+            raise ValueError("large-path seeding is restated for z-slices only")
+        llab, _ = large_labels(lab, [k for _, k in slice_list])
+        seeds = extract_seeds(data, llab, slice_list, allLabels)
+        seeds = subset_seeds(seeds, adaptive_seed_mask(llab, seeds))
+    else:
+        seeds = extract_seeds(data, lab, slice_list, allLabels)
     nol = len(allLabels)
     if mode == "reference":
         hits = walk_c(data, seeds, nbrw, sorw, key, nol, rng="ref_mrg", weight="ref_expf",
@@ -694,6 +780,8 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, smooth_iters=0, all
 
     if smooth_iters:
         sm = smooth(hits, smooth_iters, smooth_update)
+        if seeding == "large":
+            sm[0] = np.maximum(sm[0], 0)  # pycuda_large.py:440-444 clamps label 0's smoothed map at 0
         res["smooth"] = uncrop(get_labels(np.argmax(sm, axis=0).astype(np.uint8), allLabels))
     if uncertainty_map:
         res["uncertainty"] = uncrop(uncertainty(hits))

@@ -51,6 +51,17 @@ int ref_launch_walk(int variant, int gx, int gy, int gz, int segment, void* raw,
   return 0;
 }
 
+/* pycuda_large walker (adaptive seeds), launched like the small one
+ * (pycuda_large.py:404-407: block (32, 32, 1), grid (xsh/32+1, ysh/32+1, slices)). */
+int ref_launch_walk_large(int variant, int gx, int gy, int gz, int segment, void* raw, int* slices, float* a,
+                          int xsh, int ysh, int zsh, int* indices, int sorw, int nbrw) {
+  cuda_walk_fn k = variant == 0 ? ref_cuda_walk_large_i8 : ref_cuda_walk_large_f32;
+  CUDA_LAUNCH_BEGIN(gx, gy, gz)
+  k(segment, (float*)raw, slices, a, xsh, ysh, zsh, indices, sorw, nbrw);
+  CUDA_LAUNCH_END
+  return 0;
+}
+
 /* pycuda_small_allx walker (one axis per launch). */
 int ref_launch_walk_allx(int variant, int gx, int gy, int gz, int axis, int segment, void* raw, int* slices,
                          float* a, int xsh, int ysh, int zsh, int* indices, int sorw, float* beta, int nbrw) {

@@ -8,6 +8,7 @@ reference's kernel factories with stubbed pycuda/pyopencl
 JIT-compile into ``_ref/ref_sources.inc``, each wrapped in renaming macros:
   * pycuda_small._build_kernel_int8/_float32           (walkers, CUDA small path)
   * pycuda_small_allx._build_kernel_int8/_float32      (walkers, CUDA all-axis)
+  * pycuda_large._build_kernel_int8/_float32          (walkers, CUDA large path: adaptive seeds)
   * pyopencl_small._build_kernel('char'|'float','uchar') (walkers, OpenCL)
   * gpu_kernels._build_curvature_gpu/_build_update_gpu/_build_kernel_max/
     _build_kernel_uncertainty                            (post kernels)
@@ -34,6 +35,9 @@ FAST = REF / "libref_fast.so"
 _KERNELS = [
     ("biomedisa.features.random_walk.pycuda_small", "_build_kernel_int8", (), "ref_cuda_walk_i8", "Funktion"),
     ("biomedisa.features.random_walk.pycuda_small", "_build_kernel_float32", (), "ref_cuda_walk_f32", "Funktion"),
+    ("biomedisa.features.random_walk.pycuda_large", "_build_kernel_int8", (), "ref_cuda_walk_large_i8", "Funktion"),
+    ("biomedisa.features.random_walk.pycuda_large", "_build_kernel_float32", (), "ref_cuda_walk_large_f32",
+     "Funktion"),
     ("biomedisa.features.random_walk.pycuda_small_allx", "_build_kernel_int8", (), "ref_cuda_walk_allx_i8",
      "Funktion"),
     ("biomedisa.features.random_walk.pycuda_small_allx", "_build_kernel_float32", (), "ref_cuda_walk_allx_f32",

@@ -59,6 +59,17 @@ def _cases():
     lb[lb == 0] = 0
     lb[::3, 110:150, 105:145] = np.where(tb[::3, 110:150, 105:145] == 1, 1, 2)
     yield "inner_crop", big, lb, dict(base, nbrw=1, sorw=40, smooth=1)
+    # the reference large path's seed set (slice skipping, label box, adaptive seeds)
+    yield "large_seeding_inner", big, lb, dict(base, nbrw=1, sorw=40, smooth=2, seeding="large")
+    yield "large_seeding_neg_ignore", img2, lab2, dict(base, smooth=2, ignore="3", seeding="large")
+    ll = np.zeros((18, 26, 240), np.int32)
+    for z in (2, 5, 9, 13):
+        ll[z, 2:24, 3:120] = 1
+        ll[z, 2:24, 120:230] = 2
+    ll[9, 10:14, 40:60] = -1
+    ll[15] = 1
+    il = (np.random.default_rng(4).normal(90, 20, ll.shape) + 60 * (ll == 2)).clip(0, 255).astype(np.uint8)
+    yield "large_seeding_wide", il, ll, dict(base, nbrw=2, sorw=40, smooth=2, seeding="large")
 
 
 CASES = list(_cases())
@@ -72,7 +83,7 @@ def test_pipeline_bit_exact(name, img, lab, kw, cuda):
         img, lab, nbrw=kw["nbrw"], sorw=kw["sorw"], smooth_iters=kw.get("smooth", 0),
         allaxis=kw.get("allaxis", False), uncertainty_map=kw.get("uncertainty", False),
         return_hits=kw.get("return_hits", False), denoise=kw.get("denoise", False), only=kw.get("only", "all"),
-        ignore=kw.get("ignore", "none"), key=key)
+        ignore=kw.get("ignore", "none"), key=key, seeding=kw.get("seeding", "plain"))
     assert set(got) == {k for k in ("regular", "smooth", "uncertainty", "hits") if k in exp}
     for k, v in got.items():
         assert v.dtype == exp[k].dtype and v.shape == exp[k].shape, k
@@ -203,3 +214,26 @@ def test_zero_walks_and_tiny_volume(cuda):
         assert np.array_equal(r[k], e[k]), k
     r0 = smart_interpolation(img, lab, nbrw=0, sorw=10, return_hits=True)
     assert r0["hits"].sum() == 0
+
+
+def test_large_seeding_box_and_count(cuda):
+    """Large-path seeding on the wide case: the in-plane box and the number
+    of seeds kept by the adaptive filter equal the oracle's."""
+    ll = np.zeros((18, 26, 240), np.int32)
+    for z in (2, 5, 9, 13):
+        ll[z, 2:24, 3:120] = 1
+        ll[z, 2:24, 120:230] = 2
+    ll[15] = 1
+    ll[15, :, :30] = 0
+    il = np.full(ll.shape, 80, np.uint8)
+    job = _job(il, ll, seeding="large")
+    lab = np.pad(ll, 1)
+    az, bz, ay, by, ax, bx = O.predict_blocksize(lab)
+    lab = np.ascontiguousarray(lab[az:bz, ay:by, ax:bx])
+    idx = O.read_labeled_slices_large(lab)
+    llab, box = O.large_labels(lab, idx)
+    assert tuple(job.large_box) == tuple(box)
+    seeds = O.extract_seeds(np.pad(il, 1)[az:bz, ay:by, ax:bx], llab, [(0, k) for k in idx], O.pre_processing(
+        np.pad(ll, 1))[1])
+    keep = O.adaptive_seed_mask(llab, seeds)
+    assert int(job.n_seeds.item()) == int(keep.sum()) < len(keep)

@@ -153,3 +153,67 @@ def test_cc_oracle_skips_vanished_label():
     v[5:7, 5:7, 5:7] = 2
     out = C.fill(v, 0.9)
     assert (out[2:10, 2:10, 2:10] == 1).all() and not (out == 2).any()
+
+
+def _large_case():
+    """z-slices 2, 5 (skipped: within 4 of 2), 9, 13 (skipped) and 15 of an
+    18 x 26 x 240 volume: label 1 on the left, 2 on the right, a slice of label 1 only, a
+    patch of -1 (ignored) and empty columns, so that the label box, the window
+    clip (width 240 > 201) and the (row + column) % 4 lattice all matter."""
+    lab = np.zeros((18, 26, 240), np.int32)
+    for z in (2, 5, 9, 13):
+        lab[z, 2:24, 3:120] = 1
+        lab[z, 2:24, 120:230] = 2
+    lab[9, 10:14, 40:60] = -1
+    lab[15] = 1
+    rng = np.random.default_rng(4)
+    img = (rng.normal(90, 20, lab.shape) + 60 * (lab == 2)).clip(0, 255).astype(np.uint8)
+    return img, lab
+
+
+def test_large_slice_reader_matches_reference():
+    """read_labeled_slices_large of the reference vs the oracle's."""
+    import ref_import
+    _, lab = _large_case()
+    with ref_import.reference_modules():
+        import importlib
+        h = importlib.import_module("biomedisa.features.biomedisa_helper")
+        idx, _ = h.read_labeled_slices_large(np.pad(lab, 1))
+    assert idx == O.read_labeled_slices_large(np.pad(lab, 1)) == [3, 10, 16]
+
+
+@pytest.mark.skipif(not _ref_available(), reason="reference kernels not built")
+def test_large_seeding_matches_reference_large_kernel_live():
+    """The reference's large-path walker (pycuda_large.py:476-645, adaptive
+    seeds, launched as pycuda_large.py:404-407 on the reduceBlocksize stack)
+    compiled as C vs the oracle's large seeding in reference mode."""
+    import ctypes
+
+    import ref_run
+    img, lab = _large_case()
+    data = np.pad(img, 1)
+    l2 = np.pad(lab, 1)
+    _, all_labels = O.pre_processing(l2)
+    az, bz, ay, by, ax, bx = O.predict_blocksize(l2)
+    data = np.ascontiguousarray(data[az:bz, ay:by, ax:bx])
+    l2 = np.ascontiguousarray(l2[az:bz, ay:by, ax:bx])
+    idx = O.read_labeled_slices_large(l2)
+    llab, box = O.large_labels(l2, idx)
+    seeds = O.extract_seeds(data, llab, [(0, k) for k in idx], all_labels)
+    keep = O.adaptive_seed_mask(llab, seeds)
+    assert 0 < keep.sum() < len(keep)  # the filter is exercised
+    seeds = O.subset_seeds(seeds, keep)
+    hits = O.walk_c(data, seeds, 2, 40, 0, len(all_labels), rng="ref_mrg", weight="ref_expf",
+                    rng_index=seeds.rng_cuda)
+    lib = ref_run.ref_lib()
+    raw = (data.astype(np.int16) - 128).astype(np.int8)
+    Z, Y, X = data.shape
+    ind = np.asarray(idx, np.int32)
+    st = np.ascontiguousarray(llab[idx], np.int32)
+    for s, seg in enumerate(all_labels):
+        a = np.zeros((Z, Y, X), np.float32)
+        lib.ref_launch_walk_large(0, X // 32 + 1, Y // 32 + 1, len(idx), int(seg),
+                                  raw.ctypes.data_as(ctypes.c_void_p), st.ctypes.data_as(ctypes.c_void_p),
+                                  a.ctypes.data_as(ctypes.c_void_p), X, Y, Z, ind.ctypes.data_as(ctypes.c_void_p),
+                                  40, 2)
+        assert np.array_equal(a, hits[s].astype(np.float32)), f"label {seg}"
