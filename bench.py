@@ -13,7 +13,7 @@ and outputs (host->device copies and result download inside the timed region).
 ``--impl reference`` times the reference's own CPU walker on the host cores.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                       [--workload allaxis|plain|batch|large|train|hybrid]
+                       [--workload allaxis|plain|batch|large|large_ref|train|hybrid]
 """
 from __future__ import annotations
 
@@ -43,6 +43,10 @@ WORKLOADS = {
                   allaxis=False),
     "large": dict(desc="large uint8 1024^3, 6 phases, labels every 12th z-slice, nbrw=10, sorw=4000, smooth=100",
                   nbrw=10, sorw=4000, smooth=100, allaxis=False),
+    "large_ref": dict(desc="large uint8 1024^3, 6 phases, labels every 12th z-slice, nbrw=10, sorw=4000, "
+                           "smooth=100, with the reference large path's seed set (every 5th labelled slice at "
+                           "most, label box, adaptive seeds), the configuration the reference itself runs at this "
+                           "size", nbrw=10, sorw=4000, smooth=100, allaxis=False, seeding="large"),
     "train": dict(desc="surrogate training: residual 3-D CNN (16 channels, dilations 1,2,4,8, 70 k parameters), "
                        "bf16 activations/weights with fp32 accumulation, batch 8 windows of 64^3 from 16 walked "
                        "128^3 volumes (procedural and large-style), soft-target cross entropy, AdamW",
@@ -79,6 +83,8 @@ def make_batch_inputs(seed: int = 0, count: int = 32):
 def make_inputs(name: str, seed: int = 0):
     from biomedisa_gb300 import synthetic as S
 
+    if name in ("large_ref", "hybrid"):
+        name = "large"
     cache = Path(os.environ.get("SI_BENCH_CACHE", "/tmp")) / f"si_bench_{name}_{seed}.npz"
     if cache.exists():
         z = np.load(cache)
@@ -87,7 +93,7 @@ def make_inputs(name: str, seed: int = 0):
         img, lab, _ = S.allaxis_volume(seed=seed)
     elif name == "plain":
         img, lab, _ = S.plain_volume(seed=seed)
-    else:
+    else:  # large, large_ref, hybrid
         img, lab, _ = S.large_volume(seed=seed)
     try:
         np.savez(cache, img=img, lab=lab)
@@ -194,7 +200,7 @@ def run_job(img_t, img_code, lab_t, lab_code, wl, events=None):
     from biomedisa_gb300.interpolation import DeviceJob
 
     job = DeviceJob(img_t, img_code, lab_t, lab_code, nbrw=wl["nbrw"], sorw=wl["sorw"], allaxis=wl["allaxis"],
-                    smooth=wl["smooth"])
+                    smooth=wl["smooth"], seeding=wl.get("seeding", "plain"))
     msg = job.analyze()
     if msg:
         raise RuntimeError(msg)
@@ -353,7 +359,9 @@ def main():
 
     # end to end through the public API (host numpy in, numpy out)
     e2e_steps = args.e2e_steps or args.steps
-    smart_interpolation(img, lab, nbrw=wl["nbrw"], sorw=wl["sorw"], allaxis=wl["allaxis"], smooth=wl["smooth"])
+    seeding = wl.get("seeding", "plain")
+    smart_interpolation(img, lab, nbrw=wl["nbrw"], sorw=wl["sorw"], allaxis=wl["allaxis"], smooth=wl["smooth"],
+                        seeding=seeding)
     torch.cuda.synchronize()
     t_e2e = []
     out_bytes = 0
@@ -363,7 +371,7 @@ def main():
         barrier(world)
         t0 = time.perf_counter()
         r = smart_interpolation(img, lab, nbrw=wl["nbrw"], sorw=wl["sorw"], allaxis=wl["allaxis"],
-                                smooth=wl["smooth"])
+                                smooth=wl["smooth"], seeding=seeding)
         torch.cuda.synchronize()
         t_e2e.append(time.perf_counter() - t0)
         out_bytes = sum(v.nbytes for v in r.values())
