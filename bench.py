@@ -53,7 +53,7 @@ WORKLOADS = {
                   nbrw=10, sorw=4000, smooth=0, allaxis=False),
     "hybrid": dict(desc="hybrid vs plain on the large uint8 1024^3 volume (6 phases, labels every 12th z-slice, "
                         "nbrw=10, sorw=4000, smooth=0): surrogate everywhere, walk from the seeds within 8 voxels "
-                        "of voxels with max p < 0.97 (grown by 2); judge = the full plain walk",
+                        "of voxels with max p < 0.97 (grown by 2); yardstick = the full plain walk",
                    nbrw=10, sorw=4000, smooth=0, allaxis=False, threshold=0.97, radius=8, coarse=4, grow=2),
 }
 
@@ -711,7 +711,7 @@ def run_hybrid_bench(args, wl):
     img_t, lab_t = I.upload(data, labels)
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
-    # the judge: one plain job (same entry points as the large workload, smooth=0)
+    # the yardstick: one plain job (same entry points as the large workload, smooth=0)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     ev[0].record(stream)
     job, res = run_job(img_t, icode, lab_t, lcode, wl)

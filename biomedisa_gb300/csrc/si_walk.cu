@@ -20,10 +20,6 @@
 namespace si {
 namespace {
 
-__device__ __forceinline__ uint32_t pick_word(const U4& r, uint32_t sub) {
-  return sub == 0u ? r.x : (sub == 1u ? r.y : (sub == 2u ? r.z : r.w));
-}
-
 // ---------------------------------------------------------------------------
 // Packed neighbourhood records. For every interior voxel v of the working
 // volume one record holds the six neighbour intensities in move order

@@ -10,7 +10,7 @@ layer's forward and backward pass, the loss and AdamW running as hand-written
 CUDA kernels of libsmartinterp.so (bf16 activations and weights, fp32
 accumulation on the tensor cores). The hybrid interpolation walks only the
 seeds near voxels the network is unsure about and keeps the network's labels
-elsewhere; the plain walk stays the judge.
+elsewhere; the full plain walk stays the yardstick of its labels.
 
 Network: stem conv 16 -> C, B residual blocks [conv C->C (dilation d), ReLU,
 conv C->C (d), + skip, ReLU], head conv C -> 16 (logits, fp32). 3x3x3 kernels,
