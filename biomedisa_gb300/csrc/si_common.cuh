@@ -117,56 +117,77 @@ __device__ __forceinline__ float byte_plus_2p23(uint32_t w, uint32_t k) {
 }
 
 template <bool kFloat>
+__device__ __forceinline__ uint32_t walk_step(const void* __restrict__ packed_v, uint32_t pos, uint32_t bits, float c,
+                                              float bf, float b23, uint32_t* __restrict__ hl,
+                                              const int32_t* s_delta) {
+  float w0, w1, w2, w3, w4, w5;
+  uint32_t mask;
+  if (kFloat) {
+    const float4* rec = static_cast<const float4*>(packed_v) + 2 * (size_t)pos;
+    const float4 a = rec[0], b = rec[1];
+    float d;
+    d = __fsub_rn(bf, a.x); w0 = edge_weight(__fmul_rn(d, d), c);
+    d = __fsub_rn(bf, a.y); w1 = edge_weight(__fmul_rn(d, d), c);
+    d = __fsub_rn(bf, a.z); w2 = edge_weight(__fmul_rn(d, d), c);
+    d = __fsub_rn(bf, a.w); w3 = edge_weight(__fmul_rn(d, d), c);
+    d = __fsub_rn(bf, b.x); w4 = edge_weight(__fmul_rn(d, d), c);
+    d = __fsub_rn(bf, b.y); w5 = edge_weight(__fmul_rn(d, d), c);
+    mask = __float_as_uint(b.z);
+  } else {
+    const uint2 r = static_cast<const uint2*>(packed_v)[pos];
+    float d;
+    d = __fsub_rn(b23, byte_plus_2p23(r.x, 0)); w0 = edge_weight(__fmul_rn(d, d), c);
+    d = __fsub_rn(b23, byte_plus_2p23(r.x, 1)); w1 = edge_weight(__fmul_rn(d, d), c);
+    d = __fsub_rn(b23, byte_plus_2p23(r.x, 2)); w2 = edge_weight(__fmul_rn(d, d), c);
+    d = __fsub_rn(b23, byte_plus_2p23(r.x, 3)); w3 = edge_weight(__fmul_rn(d, d), c);
+    d = __fsub_rn(b23, byte_plus_2p23(r.y, 0)); w4 = edge_weight(__fmul_rn(d, d), c);
+    d = __fsub_rn(b23, byte_plus_2p23(r.y, 1)); w5 = edge_weight(__fmul_rn(d, d), c);
+    mask = r.y >> 16;
+  }
+  const float c1 = __fadd_rn(w0, w1);
+  const float c2 = __fadd_rn(c1, w2);
+  const float c3 = __fadd_rn(c2, w3);
+  const float c4 = __fadd_rn(c3, w4);
+  const float c5 = __fadd_rn(c4, w5);
+  const float rnd = __fmul_rn(c5, u01_from_bits(bits));
+  int dir = (int)(w0 <= rnd) + (int)(c1 <= rnd) + (int)(c2 <= rnd) + (int)(c3 <= rnd) + (int)(c4 <= rnd);
+  if (rnd == 0.0f) dir = 0;
+  if (!((mask >> dir) & 1u)) {
+    pos += (uint32_t)s_delta[dir];
+    atomicAdd(&hl[pos], 1u);
+  }
+  return pos;
+}
+
+__device__ __forceinline__ uint32_t philox_word(const U4& r, uint32_t sub) {
+  return sub == 0u ? r.x : (sub == 1u ? r.y : (sub == 2u ? r.z : r.w));
+}
+
+// Steps t in [t, t_end): step t uses word (t & 3) of the Philox block t >> 2.
+// Aligned groups of four steps share one block evaluation; the unaligned head
+// and tail take their words one by one (same words, same order).
+template <bool kFloat>
 __device__ __forceinline__ uint32_t walk_steps(const void* __restrict__ packed_v, uint32_t pos, uint32_t t,
                                                uint32_t t_end, float c, float bf, uint32_t seed_pos,
                                                uint32_t axis, uint32_t label, uint32_t k0, uint32_t k1,
                                                uint32_t* __restrict__ hl, const int32_t* s_delta) {
   const float b23 = __fadd_rn(bf, 8388608.0f);  // 2^23 + B, exact for uint8 B
-  uint32_t blk = t >> 2;
-  U4 rr = philox4x32_10(U4{blk, seed_pos, axis, label}, k0, k1);
-  for (; t < t_end; ++t) {
-    if ((t >> 2) != blk) {
-      blk = t >> 2;
-      rr = philox4x32_10(U4{blk, seed_pos, axis, label}, k0, k1);
-    }
-    const uint32_t sub = t & 3u;
-    const uint32_t bits = sub == 0u ? rr.x : (sub == 1u ? rr.y : (sub == 2u ? rr.z : rr.w));
-    float w0, w1, w2, w3, w4, w5;
-    uint32_t mask;
-    if (kFloat) {
-      const float4* rec = static_cast<const float4*>(packed_v) + 2 * (size_t)pos;
-      const float4 a = rec[0], b = rec[1];
-      float d;
-      d = __fsub_rn(bf, a.x); w0 = edge_weight(__fmul_rn(d, d), c);
-      d = __fsub_rn(bf, a.y); w1 = edge_weight(__fmul_rn(d, d), c);
-      d = __fsub_rn(bf, a.z); w2 = edge_weight(__fmul_rn(d, d), c);
-      d = __fsub_rn(bf, a.w); w3 = edge_weight(__fmul_rn(d, d), c);
-      d = __fsub_rn(bf, b.x); w4 = edge_weight(__fmul_rn(d, d), c);
-      d = __fsub_rn(bf, b.y); w5 = edge_weight(__fmul_rn(d, d), c);
-      mask = __float_as_uint(b.z);
-    } else {
-      const uint2 r = static_cast<const uint2*>(packed_v)[pos];
-      float d;
-      d = __fsub_rn(b23, byte_plus_2p23(r.x, 0)); w0 = edge_weight(__fmul_rn(d, d), c);
-      d = __fsub_rn(b23, byte_plus_2p23(r.x, 1)); w1 = edge_weight(__fmul_rn(d, d), c);
-      d = __fsub_rn(b23, byte_plus_2p23(r.x, 2)); w2 = edge_weight(__fmul_rn(d, d), c);
-      d = __fsub_rn(b23, byte_plus_2p23(r.x, 3)); w3 = edge_weight(__fmul_rn(d, d), c);
-      d = __fsub_rn(b23, byte_plus_2p23(r.y, 0)); w4 = edge_weight(__fmul_rn(d, d), c);
-      d = __fsub_rn(b23, byte_plus_2p23(r.y, 1)); w5 = edge_weight(__fmul_rn(d, d), c);
-      mask = r.y >> 16;
-    }
-    const float c1 = __fadd_rn(w0, w1);
-    const float c2 = __fadd_rn(c1, w2);
-    const float c3 = __fadd_rn(c2, w3);
-    const float c4 = __fadd_rn(c3, w4);
-    const float c5 = __fadd_rn(c4, w5);
-    const float rnd = __fmul_rn(c5, u01_from_bits(bits));
-    int dir = (int)(w0 <= rnd) + (int)(c1 <= rnd) + (int)(c2 <= rnd) + (int)(c3 <= rnd) + (int)(c4 <= rnd);
-    if (rnd == 0.0f) dir = 0;
-    if (!((mask >> dir) & 1u)) {
-      pos += (uint32_t)s_delta[dir];
-      atomicAdd(&hl[pos], 1u);
-    }
+  if ((t & 3u) && t < t_end) {
+    const U4 rr = philox4x32_10(U4{t >> 2, seed_pos, axis, label}, k0, k1);
+    for (; (t & 3u) && t < t_end; ++t)
+      pos = walk_step<kFloat>(packed_v, pos, philox_word(rr, t & 3u), c, bf, b23, hl, s_delta);
+  }
+  for (; t + 4u <= t_end; t += 4u) {
+    const U4 rr = philox4x32_10(U4{t >> 2, seed_pos, axis, label}, k0, k1);
+    pos = walk_step<kFloat>(packed_v, pos, rr.x, c, bf, b23, hl, s_delta);
+    pos = walk_step<kFloat>(packed_v, pos, rr.y, c, bf, b23, hl, s_delta);
+    pos = walk_step<kFloat>(packed_v, pos, rr.z, c, bf, b23, hl, s_delta);
+    pos = walk_step<kFloat>(packed_v, pos, rr.w, c, bf, b23, hl, s_delta);
+  }
+  if (t < t_end) {
+    const U4 rr = philox4x32_10(U4{t >> 2, seed_pos, axis, label}, k0, k1);
+    for (; t < t_end; ++t)
+      pos = walk_step<kFloat>(packed_v, pos, philox_word(rr, t & 3u), c, bf, b23, hl, s_delta);
   }
   return pos;
 }
