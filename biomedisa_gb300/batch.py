@@ -88,8 +88,29 @@ def run_device_batch(device_volumes, nbrw=10, sorw=4000, smooth=0, allaxis=False
     return jobs, results, rep
 
 
-def walk_batch(jobs, nbrw, sorw, rng_seed, sort_edge=0, sweep_steps=0, tune=True):
-    """One batched walk over all prepared jobs. Returns a report dict."""
+GROUP_WALKS = 1 << 25  # walks per group of consecutive volumes (compact working set per sweep)
+
+
+def volume_groups(seeds, nbrw, group_walks=GROUP_WALKS):
+    """Consecutive volume index ranges holding about group_walks walks each
+    (a volume is never split)."""
+    groups, start, acc = [], 0, 0
+    for k, n in enumerate(seeds):
+        acc += n * nbrw
+        if acc >= group_walks:
+            groups.append((start, k + 1))
+            start, acc = k + 1, 0
+    if start < len(seeds):
+        groups.append((start, len(seeds)))
+    return groups
+
+
+def walk_batch(jobs, nbrw, sorw, rng_seed, sort_edge=0, sweep_steps=0, tune=True, group_walks=GROUP_WALKS):
+    """Batched walk over all prepared jobs: volumes are walked in groups of
+    consecutive volumes of about group_walks walks, all labels and volumes of
+    a group sharing every launch (si_walk_sorted_batch). Hits are integer sums
+    of independent walks, so the grouping does not change them. Returns a
+    report dict."""
     live = [j for j in jobs if j is not None]
     if not live:
         return {}
@@ -98,21 +119,31 @@ def walk_batch(jobs, nbrw, sorw, rng_seed, sort_edge=0, sweep_steps=0, tune=True
         cp = j.cplan
         arr[k] = SiVolume(_ptr(j.packed), _ptr(j.hits), _ptr(j.seeds), _ptr(j.n_seeds), j.seed_capacity, cp.Zc,
                           cp.Yc, cp.Xc, j.lplan.nol, int(j.work_is_float))
-    walks = sum(int(j.n_seeds.item()) for j in live) * nbrw
+    seeds = [int(j.n_seeds.item()) for j in live]
+    walks = sum(seeds) * nbrw
     report = {}
     if tune and not (sort_edge and sweep_steps):
         sort_edge, sweep_steps, report = autotune.tune(arr, len(live), [j.hits for j in live], nbrw, sorw,
                                                         rng_seed, walks)
-    need = ctypes.c_ulonglong(0)
-    nat.call("si_walk_sorted_batch_scratch", arr, len(live), nbrw, sort_edge, ctypes.byref(need))
-    scratch = torch.empty(max(int(need.value), 1), dtype=torch.uint8, device="cuda")
-    rounds = ctypes.c_int(0)
-    nat.call("si_walk_sorted_batch", arr, len(live), nbrw, sorw, rng_seed, sweep_steps, sort_edge,
-             _ptr(scratch), int(need.value), ctypes.byref(rounds), _stream())
+    groups = volume_groups(seeds, nbrw, group_walks) if group_walks else [(0, len(live))]
+    size = ctypes.sizeof(SiVolume)
+    need_max = 0
+    for a, b in groups:
+        need = ctypes.c_ulonglong(0)
+        nat.call("si_walk_sorted_batch_scratch", ctypes.byref(arr, a * size), b - a, nbrw, sort_edge,
+                 ctypes.byref(need))
+        need_max = max(need_max, int(need.value))
+    scratch = torch.empty(max(need_max, 1), dtype=torch.uint8, device="cuda")
+    total_rounds = 0
+    for a, b in groups:
+        rounds = ctypes.c_int(0)
+        nat.call("si_walk_sorted_batch", ctypes.byref(arr, a * size), b - a, nbrw, sorw, rng_seed, sweep_steps,
+                 sort_edge, _ptr(scratch), need_max, ctypes.byref(rounds), _stream())
+        total_rounds += int(rounds.value)
     for j in live:
-        j.rounds = int(rounds.value)
-    report.update({"sort_edge": sort_edge, "sweep_steps": sweep_steps, "sweeps": int(rounds.value),
-                   "walker_steps": walks * sorw})
+        j.rounds = total_rounds
+    report.update({"sort_edge": sort_edge, "sweep_steps": sweep_steps, "sweeps": total_rounds,
+                   "walker_steps": walks * sorw, "volume_groups": len(groups)})
     return report
 
 
