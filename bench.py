@@ -6,6 +6,11 @@ every 16th YZ/XZ slice, nbrw=10, sorw=4000, smooth=100 — on device-resident
 inputs: label analysis, working image, seed extraction, the walk, argmax,
 100 smoothing iterations per label and the smoothed argmax.
 
+Other workloads (--workload): plain (128^3), large (1024^3), large_ref
+(1024^3 with the reference large path's seed set), batch (32 uneven uint16
+volumes in one batched walk), train (surrogate training voxels/s), hybrid
+(surrogate + restricted walk vs the plain walk at 1024^3, voxels/s).
+
 Metric: walker-steps/s = (seeds * nbrw * sorw) / step time (whole job).
 ``e2e`` is the same metric through ``smart_interpolation`` with numpy inputs
 and outputs (host->device copies and result download inside the timed region).

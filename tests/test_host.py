@@ -1,0 +1,76 @@
+"""Host-side planning logic (no GPU): label plans, crops, the large path's
+slice list, volume groups of the batched walk, slot permutations of the
+surrogate's training."""
+import numpy as np
+
+from biomedisa_gb300 import interpolation as I
+from biomedisa_gb300.batch import volume_groups
+import oracle as O
+
+
+def test_large_slice_list_matches_oracle():
+    rng = np.random.default_rng(0)
+    for _ in range(20):
+        zs = np.sort(rng.choice(60, size=rng.integers(1, 25), replace=False))
+        lab = np.zeros((60, 4, 4), np.int32)
+        lab[zs, 1, 1] = 1
+        sl = np.asarray([(0, int(z)) for z in zs], np.int32)
+        got = [int(z) for _, z in I.large_slice_list(sl).tolist()]
+        assert got == O.read_labeled_slices_large(lab)
+
+
+def test_large_slice_list_keeps_z_only():
+    sl = np.asarray([(0, 2), (0, 4), (0, 8), (1, 3), (2, 5)], np.int32)
+    assert I.large_slice_list(sl).tolist() == [[0, 2], [0, 8]]
+
+
+def test_volume_groups_cover_in_order():
+    rng = np.random.default_rng(1)
+    for _ in range(50):
+        seeds = rng.integers(0, 5_000_000, size=rng.integers(1, 40)).tolist()
+        groups = volume_groups(seeds, 10, group_walks=1 << 25)
+        flat = [k for a, b in groups for k in range(a, b)]
+        assert flat == list(range(len(seeds)))
+        for a, b in groups[:-1]:
+            assert sum(seeds[a:b]) * 10 >= 1 << 25
+            assert sum(seeds[a:b - 1]) * 10 < 1 << 25
+
+
+def test_plan_labels_only_ignore():
+    hist = np.zeros(258, np.int64)
+    hist[[0, 1, 2, 5]] = 10
+    hist[256] = 3  # negatives
+    p = I.plan_labels(hist, only="1,5")
+    assert p.all_labels.tolist() == [0, 1, 5]
+    assert p.slot_lut[2] == 0 and p.slot_lut[5] == 2 and p.slot_lut[1] == 1
+    q = I.plan_labels(hist, ignore="2")
+    assert q.all_labels.tolist() == [0, 1, 5] and q.slot_lut[2] == 0
+
+
+def test_plan_crop_matches_predict_blocksize():
+    rng = np.random.default_rng(2)
+    for _ in range(10):
+        shape = tuple(int(v) for v in rng.integers(5, 300, 3))
+        lab = np.zeros(shape, np.int32)
+        z = rng.integers(0, shape[0]); y0, y1 = sorted(rng.integers(0, shape[1], 2)); x0, x1 = sorted(
+            rng.integers(0, shape[2], 2))
+        lab[z, y0:y1 + 1, x0:x1 + 1] = 1
+        padded = np.pad(lab, 1)
+        az, bz, ay, by, ax, bx = O.predict_blocksize(padded)
+        flags = [np.zeros(s + 2, np.uint8) for s in shape]
+        flags[0][z + 1] = 1
+        bbox = (z + 1, z + 1, y0 + 1, y1 + 1, x0 + 1, x1 + 1)
+        cp = I.plan_crop(shape, bbox, flags, False)
+        assert (cp.cz0, cp.cz0 + cp.Zc, cp.cy0, cp.cy0 + cp.Yc, cp.cx0, cp.cx0 + cp.Xc) == (az, bz, ay, by, ax, bx)
+        assert cp.slice_list.tolist() == [[0, z + 1 - az]]
+
+
+def test_slot_permutation_keeps_slot_zero():
+    from biomedisa_gb300.surrogate import MAX_SLOTS, _slot_permutation
+    rng = np.random.default_rng(3)
+    for nol in range(1, MAX_SLOTS + 1):
+        src, dst = _slot_permutation(rng, nol)
+        assert dst[0] == 0 and len(set(dst.tolist())) == nol
+        new = np.arange(16)[src]
+        for k in range(nol):
+            assert new[3 + dst[k]] == 3 + k
