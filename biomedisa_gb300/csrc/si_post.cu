@@ -162,15 +162,31 @@ __global__ void __launch_bounds__(kTX * kTY) smooth_tile_kernel(const void* __re
   const size_t X = (size_t)Xc, F = (size_t)Yc * Xc;
   const int x = x0 + tx, y = y0 + ty;
   const int tid = ty * kTX + tx;
-  // loads plane z (clamped to the volume; outside values are never used) into slot s
-  auto load_plane = [&](int z, int sidx) {
-    for (int i = tid; i < (kTY + 2) * (kTX + 2); i += kTX * kTY) {
+  // Each thread fills at most two halo-tile entries per plane; their tile and
+  // in-plane offsets are fixed for the whole z-loop (kLoads: ceil(340 / 256)).
+  constexpr int kTile = (kTY + 2) * (kTX + 2), kLoads = (kTile + kTX * kTY - 1) / (kTX * kTY);
+  int tile_idx[kLoads];
+  int64_t plane_off[kLoads];  // -1: outside the plane (or no entry)
+#pragma unroll
+  for (int k = 0; k < kLoads; ++k) {
+    const int i = tid + k * kTX * kTY;
+    tile_idx[k] = i;
+    plane_off[k] = -1;
+    if (i < kTile) {
       const int ly = i / (kTX + 2), lx = i - ly * (kTX + 2);
       const int gy = y0 + ly - 1, gx = x0 + lx - 1;
-      float v = 0.0f;
-      if (z >= 0 && z < Zc && gy >= 0 && gy < Yc && gx >= 0 && gx < Xc)
-        v = ld<kSrcU32>(src, (size_t)z * F + (size_t)gy * X + gx);
-      pl[sidx][ly][lx] = v;
+      if (gy >= 0 && gy < Yc && gx >= 0 && gx < Xc) plane_off[k] = (int64_t)gy * X + gx;
+    }
+  }
+  // loads plane z (zero outside the volume; such values are never used) into slot sidx
+  auto load_plane = [&](int z, int sidx) {
+    float* dstp = &pl[sidx][0][0];
+    const bool zin = z >= 0 && z < Zc;
+#pragma unroll
+    for (int k = 0; k < kLoads; ++k) {
+      if (tile_idx[k] < kTile)
+        dstp[tile_idx[k]] = (zin && plane_off[k] >= 0) ? ld<kSrcU32>(src, (size_t)z * F + (size_t)plane_off[k])
+                                                       : 0.0f;
     }
   };
   load_plane(zb - 1, 0);
