@@ -6,7 +6,8 @@ every 16th YZ/XZ slice, nbrw=10, sorw=4000, smooth=100 — on device-resident
 inputs: label analysis, working image, seed extraction, the walk, argmax,
 100 smoothing iterations per label and the smoothed argmax.
 
-Other workloads (--workload): plain (128^3), large (1024^3), large_ref
+Other workloads (--workload): plain (128^3), screw (419x492x462, the shape and
+labelling of the reference's published timing case), large (1024^3), large_ref
 (1024^3 with the reference large path's seed set), batch (32 uneven uint16
 volumes in one batched walk), train (surrogate training voxels/s), hybrid
 (surrogate + restricted walk vs the plain walk at 1024^3, voxels/s).
@@ -18,7 +19,7 @@ and outputs (host->device copies and result download inside the timed region).
 ``--impl reference`` times the reference's own CPU walker on the host cores.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                       [--workload allaxis|plain|batch|large|large_ref|train|hybrid]
+                       [--workload allaxis|plain|screw|batch|large|large_ref|train|hybrid]
 """
 from __future__ import annotations
 
@@ -48,6 +49,9 @@ WORKLOADS = {
                   allaxis=False),
     "large": dict(desc="large uint8 1024^3, 6 phases, labels every 12th z-slice, nbrw=10, sorw=4000, smooth=100",
                   nbrw=10, sorw=4000, smooth=100, allaxis=False),
+    "screw": dict(desc="screw-like uint8 (z,y,x)=(419,492,462), 2 objects labelled every 20th z-slice, nbrw=10, "
+                       "sorw=4000, smooth=0: the dimensions and labelling of the reference's published end-to-end "
+                       "timing case (synthetic content)", nbrw=10, sorw=4000, smooth=0, allaxis=False),
     "large_ref": dict(desc="large uint8 1024^3, 6 phases, labels every 12th z-slice, nbrw=10, sorw=4000, "
                            "smooth=100, with the reference large path's seed set (every 5th labelled slice at "
                            "most, label box, adaptive seeds), the configuration the reference itself runs at this "
@@ -98,6 +102,8 @@ def make_inputs(name: str, seed: int = 0):
         img, lab, _ = S.allaxis_volume(seed=seed)
     elif name == "plain":
         img, lab, _ = S.plain_volume(seed=seed)
+    elif name == "screw":
+        img, lab, _ = S.screw_like_volume(seed=seed)
     else:  # large, large_ref, hybrid
         img, lab, _ = S.large_volume(seed=seed)
     try:

@@ -12,6 +12,9 @@ from numpy.random.default_rng(seed):
     phases and label spacing 4..20;
   * ``large_volume``   1024^3 uint8 with 6 phases, uint8 labels on every 12th
     XY slice.
+  * ``screw_like_volume`` 419x492x462 uint8 with 2 objects labelled every 20th
+    z-slice (the dimensions and labelling of the reference's published
+    "biological screw" timing; synthetic content).
 Each generator returns (image, sparse labels, ground truth).
 """
 from __future__ import annotations
@@ -213,3 +216,16 @@ def procedural_volume(rng, shape=(96, 96, 96)):
     np.clip(img, 0, 255, out=img)
     every = int(rng.integers(6, 15))
     return np.rint(img).astype(np.uint8), sparse_labels(truth, z_every=every), truth
+
+
+def screw_like_volume(seed=0, shape=(419, 492, 462), z_every=20):
+    """Dimensions and labelling of the reference's published end-to-end timing
+    case (419x492x462, 2 objects labelled on every 20th slice) with synthetic
+    content: a tube (screw shaft) and an ellipsoid, noise sigma 12."""
+    rng = np.random.default_rng(seed)
+    truth = np.zeros(shape, np.uint8)
+    Z, Y, X = shape
+    _paint_tube(truth, 1, (0.1 * Z, 0.5 * Y, 0.45 * X), (0.9 * Z, 0.5 * Y, 0.55 * X), 0.15 * min(Y, X))
+    _paint_ellipsoid(truth, 2, (0.5 * Z, 0.3 * Y, 0.7 * X), (0.2 * Z, 0.12 * Y, 0.12 * X), _rotation(rng))
+    img = _render(truth, (150, 210), 40, 12.0, rng)
+    return img, sparse_labels(truth, z_every=z_every), truth
