@@ -401,13 +401,14 @@ def main():
     l2_gbs = l2["read_gbs"]
     achieved_payload = walk_rate * WALK_BYTES_PAYLOAD_U8 / 1e9
     achieved_l2 = walk_rate * WALK_SECTORS_L2 * 32 / 1e9
-    traffic = None
+    traffic, traffic_per_step = None, None
     sweeps = max(getattr(job, "rounds", 0) or 0, 1)
     tp = ROOT / "profiles" / "walker_traffic.json"
     if tp.exists():
         tj = json.loads(tp.read_text())
         if tj.get("workload") == args.workload:
-            traffic = tj["dram_bytes_per_step"] * steps_per_job / sweeps  # DRAM bytes per sweep launch
+            traffic_per_step = tj["dram_bytes_per_step"]
+            traffic = traffic_per_step * steps_per_job / sweeps  # DRAM bytes per sweep launch
 
     line = {
         "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": world, "steps": args.steps,
@@ -426,7 +427,7 @@ def main():
                              f"{WALK_BYTES_PAYLOAD_U8} B/step logical payload (6 neighbour bytes + 4-byte hit) x "
                              f"steps / CUDA-event walk duration; peak {peak_kind} (MEASURED_PEAKS.json hbm_gbs); "
                              "traffic = DRAM bytes per sweep launch from profiles/sweep_kernel_allaxis.md "
-                             "(10.88 B/step, scaled by steps per launch)"},
+                             f"({traffic_per_step} B/step, scaled by steps per launch)"},
         "roofline_l2": {"bound": "l2", "achieved": achieved_l2, "peak": l2_gbs, "unit": "GB/s",
                         "frac": achieved_l2 / l2_gbs if l2_gbs else None,
                         "atomics_per_s": walk_rate, "atomic_peak_per_s": l2["atomics_per_s"],
