@@ -218,3 +218,39 @@ def test_hybrid_gain_over_untrained(cuda):
     assert st["frac_seeds_walked"] < 0.75
     assert st["walker_steps"] < 0.75 * job.total_steps()
     assert min(dice.values()) >= 0.97
+
+
+def test_smooth_f32_matches_oracle(cuda):
+    """si_smooth_f32 (smoothing of the hybrid's float probability maps) equals
+    the oracle's smoothing of the same maps bit for bit."""
+    import oracle as O
+    from biomedisa_gb300 import _native as nat
+    rng = np.random.default_rng(9)
+    maps = rng.random((3, 19, 23, 37)).astype(np.float32)
+    maps[:, 5:9] *= 4.0
+    t = torch.from_numpy(maps.copy()).to(cuda)
+    V = maps[0].size
+    tmp0 = torch.empty(V, dtype=torch.float32, device=cuda)
+    tmp1 = torch.empty(V, dtype=torch.float32, device=cuda)
+    for iters in (1, 4):
+        t.copy_(torch.from_numpy(maps))
+        nat.call("si_smooth_f32", t.data_ptr(), tmp0.data_ptr(), tmp1.data_ptr(), 3, 19, 23, 37, iters,
+                 torch.cuda.current_stream().cuda_stream)
+        assert np.array_equal(t.cpu().numpy(), O.smooth(maps, iters, "f32")), iters
+
+
+def test_hybrid_smooth_and_keys(cuda):
+    """The hybrid with smoothing returns regular and smooth label volumes of
+    the input shape; an untrained network walks every seed, so on every voxel
+    a walk reached its regular result equals the plain walk's."""
+    from biomedisa_gb300 import smart_interpolation
+    from biomedisa_gb300.synthetic import plain_volume
+    img, lab, _ = plain_volume(seed=3, shape=(40, 44, 48), z_every=6, semi=(7, 14))
+    net = S.SurrogateNet(seed=2)
+    res, st = S.hybrid_interpolation(img, lab, net, nbrw=3, sorw=100, smooth=3)
+    plain = smart_interpolation(img, lab, nbrw=3, sorw=100, return_hits=True)
+    assert set(res) >= {"regular", "smooth"} and res["smooth"].shape == img.shape
+    assert st["frac_seeds_walked"] == 1.0
+    reached = plain["hits"].sum(0) > 0
+    assert reached.mean() > 0.5
+    assert np.array_equal(res["regular"].cpu().numpy()[reached], plain["regular"][reached])
