@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(128) conv3d_fwd_kernel(const __nv_bfloat16* __
 constexpr int kC16Warps = 4;
 
 template <bool kOutF32>
-__global__ void __launch_bounds__(kC16Warps * 32) conv16_kernel(const __nv_bfloat16* __restrict__ x,
+__global__ void __launch_bounds__(kC16Warps * 32, 4) conv16_kernel(const __nv_bfloat16* __restrict__ x,
                                                                 const __nv_bfloat16* __restrict__ w,
                                                                 const float* __restrict__ bias,
                                                                 const __nv_bfloat16* __restrict__ residual,
