@@ -178,28 +178,40 @@ __global__ void __launch_bounds__(kTX * kTY) smooth_tile_kernel(const void* __re
       if (gy >= 0 && gy < Yc && gx >= 0 && gx < Xc) plane_off[k] = (int64_t)gy * X + gx;
     }
   }
-  // loads plane z (zero outside the volume; such values are never used) into slot sidx
-  auto load_plane = [&](int z, int sidx) {
+  // loads plane z (zero outside the volume; such values are never used) into
+  // slot sidx and returns the OR of the bit patterns this thread stored
+  auto load_plane = [&](int z, int sidx) -> uint32_t {
     float* dstp = &pl[sidx][0][0];
     const bool zin = z >= 0 && z < Zc;
+    uint32_t orv = 0u;
 #pragma unroll
     for (int k = 0; k < kLoads; ++k) {
-      if (tile_idx[k] < kTile)
-        dstp[tile_idx[k]] = (zin && plane_off[k] >= 0) ? ld<kSrcU32>(src, (size_t)z * F + (size_t)plane_off[k])
-                                                       : 0.0f;
+      if (tile_idx[k] < kTile) {
+        const float v = (zin && plane_off[k] >= 0) ? ld<kSrcU32>(src, (size_t)z * F + (size_t)plane_off[k]) : 0.0f;
+        dstp[tile_idx[k]] = v;
+        orv |= __float_as_uint(v);
+      }
     }
+    return orv;
   };
-  load_plane(zb - 1, 0);
-  load_plane(zb, 1);
+  // A plane flag is set when any value of the tile's (halo) plane is not +0.0.
+  // When the three planes around z are all +0.0, every stencil of the tile
+  // is +0 and stays exactly +0 (all differences 0, num = +0, +0 / (0 + 1e-10)
+  // = +0), so the block writes the centre values and skips the arithmetic;
+  // hit maps are +0 far from their label's region.
+  int nzm = __syncthreads_or(load_plane(zb - 1, 0) != 0u);
+  int nz0 = __syncthreads_or(load_plane(zb, 1) != 0u);
   int sm = 0, s0 = 1, sp = 2;
   for (int z = zb; z < ze; ++z) {
-    load_plane(z + 1, sp);
-    __syncthreads();
-    if (x < Xc && y < Yc) {
-      const int lx = tx + 1, ly = ty + 1;
+    const int nzp = __syncthreads_or(load_plane(z + 1, sp) != 0u);
+    const bool quiet = !(nzm | nz0 | nzp);
+    const int lx = tx + 1, ly = ty + 1;
+    const bool inside = x < Xc && y < Yc;
+    const bool interior = inside && z > 0 && y > 0 && x > 0 && z < Zc - 1 && y < Yc - 1 && x < Xc - 1;
+    if (inside) {
       const float c = pl[s0][ly][lx];
       const size_t i = (size_t)z * F + (size_t)y * X + x;
-      if (!(z > 0 && y > 0 && x > 0 && z < Zc - 1 && y < Yc - 1 && x < Xc - 1)) {
+      if (quiet || !interior) {
         dst[i] = c;
       } else {
         const float c2 = __fmul_rn(2.0f, c);
@@ -241,6 +253,8 @@ __global__ void __launch_bounds__(kTX * kTY) smooth_tile_kernel(const void* __re
     sm = s0;
     s0 = sp;
     sp = t;
+    nzm = nz0;
+    nz0 = nzp;
   }
 }
 
