@@ -77,10 +77,13 @@ def xent(logits, target, weight, nol):
     return loss, g
 
 
-def network_grads(x, ws, bs, dils, target, weight, nol):
+def network_grads(x, ws, bs, dils, target, weight, nol, rounding=True):
     """Forward + backward of the surrogate network (stem, residual blocks,
-    head) with bf16 rounding of stored activations; returns (loss, logits,
-    [dW], [db])."""
+    head) with bf16 rounding of stored activations and gradients and fp32
+    logits, as the GPU stores them; returns (loss, logits, [dW], [db]).
+    rounding=False keeps everything in float64 (exact derivatives of the
+    loss, for finite-difference checks of the oracle itself)."""
+    bf16_round = globals()["bf16_round"] if rounding else (lambda a: np.asarray(a, np.float64))
     acts = [x]
     a = bf16_round(np.maximum(conv_fwd(x, ws[0], bs[0]), 0))
     acts.append(a)
@@ -88,7 +91,9 @@ def network_grads(x, ws, bs, dils, target, weight, nol):
         t = bf16_round(np.maximum(conv_fwd(a, ws[1 + 2 * i], bs[1 + 2 * i], d), 0))
         a = bf16_round(np.maximum(conv_fwd(t, ws[2 + 2 * i], bs[2 + 2 * i], d) + a, 0))
         acts += [t, a]
-    logits = conv_fwd(a, ws[-1], bs[-1]).astype(np.float32).astype(np.float64)
+    logits = conv_fwd(a, ws[-1], bs[-1])
+    if rounding:
+        logits = logits.astype(np.float32).astype(np.float64)
     loss, dl = xent(logits, target, weight, nol)
     dl = bf16_round(dl)
     dws, dbs = [None] * len(ws), [None] * len(ws)
