@@ -42,3 +42,25 @@ def test_argument_errors_without_launch(native_lib):
     rc = native_lib.si_smooth(None, None, None, 1, 4, 4, 4, 1, None)
     assert rc == 1
     assert _native.SI_F32 == 5
+
+
+def declared_arities():
+    """Parameter count of every si_* declaration in the header."""
+    text = (ROOT / "include" / "smartinterp.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(si_\w+)\s*\(([^;{]*?)\)\s*;", text, re.S):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_binding_arities_match_header():
+    """Every ctypes argument list has as many entries as the header's
+    declaration has parameters (a drifted signature would pass garbage)."""
+    from biomedisa_gb300 import _native
+
+    ar = declared_arities()
+    assert set(_native._SIGNATURES) <= set(ar)
+    for name, args in _native._SIGNATURES.items():
+        assert len(args) == ar[name], (name, len(args), ar[name])
