@@ -22,6 +22,29 @@ def test_philox_numpy_python_c_agree(c_oracle):
         assert np.array_equal(a, b) and np.array_equal(a, c)
 
 
+# Philox4x32-10 known answers (Salmon et al., SC'11; the Random123 test
+# vectors): (counter, key) -> output.
+PHILOX_KAT = [
+    ((0x00000000, 0x00000000, 0x00000000, 0x00000000), (0x00000000, 0x00000000),
+     (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+    ((0xFFFFFFFF, 0xFFFFFFFF, 0xFFFFFFFF, 0xFFFFFFFF), (0xFFFFFFFF, 0xFFFFFFFF),
+     (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+    ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+     (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)),
+]
+
+
+def test_philox_known_answers(c_oracle):
+    for ctr, key, out in PHILOX_KAT:
+        assert tuple(O.philox_python(ctr, key)) == out
+        a = O.philox4x32_10(*(np.array([v], np.uint32) for v in ctr), *key)
+        assert tuple(int(w[0]) for w in a) == out
+        c_in = np.array([ctr], np.uint32)
+        c_out = np.zeros_like(c_in)
+        c_oracle.or_philox(c_in.ctypes.data, key[0], key[1], c_out.ctypes.data, 1)
+        assert tuple(int(v) for v in c_out[0]) == out
+
+
 def test_philox_uniformity():
     """u01 of a Philox stream: mean 1/2, variance 1/12, flat histogram."""
     n = 1 << 18
