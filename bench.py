@@ -10,7 +10,8 @@ Other workloads (--workload): plain (128^3), screw (419x492x462, the shape and
 labelling of the reference's published timing case), large (1024^3), large_ref
 (1024^3 with the reference large path's seed set), batch (32 uneven uint16
 volumes in one batched walk), train (surrogate training voxels/s), hybrid
-(surrogate + restricted walk vs the plain walk at 1024^3, voxels/s).
+(surrogate + restricted walk vs the plain walk at 1024^3, voxels/s), geodesic
+(geodesic raster-scan interpolation of the plain volume, voxels/s).
 
 Metric: walker-steps/s = (seeds * nbrw * sorw) / step time (whole job).
 ``e2e`` is the same metric through ``smart_interpolation`` with numpy inputs
@@ -19,7 +20,7 @@ and outputs (host->device copies and result download inside the timed region).
 ``--impl reference`` times the reference's own CPU walker on the host cores.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                       [--workload allaxis|plain|screw|batch|large|large_ref|train|hybrid]
+                       [--workload allaxis|plain|screw|batch|large|large_ref|train|hybrid|geodesic]
 """
 from __future__ import annotations
 
@@ -64,6 +65,9 @@ WORKLOADS = {
                         "nbrw=10, sorw=4000, smooth=0): surrogate everywhere, walk from the seeds within 8 voxels "
                         "of voxels with max p < 0.97 (grown by 2); yardstick = the full plain walk",
                    nbrw=10, sorw=4000, smooth=0, allaxis=False, threshold=0.97, radius=8, coarse=4, grow=2),
+    "geodesic": dict(desc="geodesic interpolation (geodis.geodesic_segment: lamb=1.0, 4 forward+backward raster "
+                          "iterations per label) of the plain uint8 128^3 volume, labels 0..2 on every 10th z-slice",
+                     nbrw=0, sorw=0, smooth=0, allaxis=False),
 }
 
 # one kernel per entry-point call except these (launches per call)
@@ -94,6 +98,8 @@ def make_inputs(name: str, seed: int = 0):
 
     if name in ("large_ref", "hybrid"):
         name = "large"
+    if name == "geodesic":
+        name = "plain"
     cache = Path(os.environ.get("SI_BENCH_CACHE", "/tmp")) / f"si_bench_{name}_{seed}.npz"
     if cache.exists():
         z = np.load(cache)
@@ -326,6 +332,9 @@ def main():
         return
     if args.workload == "hybrid":
         run_hybrid_bench(args, wl)
+        return
+    if args.workload == "geodesic":
+        run_geodesic_bench(args, wl)
         return
     if args.impl == "reference":
         run_reference(args, wl)
@@ -813,6 +822,143 @@ def run_hybrid_bench(args, wl):
                                     "sample": f"unavailable: {ex}"}
     if rank == 0:
         print(json.dumps(line))
+
+
+def geo_wave_launches(shape, iterations=4):
+    """Wavefront launches of one si_geo_scan call (both passes, all iterations),
+    from the library's own launch plan."""
+    import ctypes
+
+    from biomedisa_gb300 import _native as nat
+
+    n = 0
+    t = np.empty(shape, np.int32)
+    for fwd in (1, 0):
+        if nat.lib().si_geo_visit_order(*shape, fwd, t.ctypes.data_as(ctypes.c_void_p)) != 0:
+            raise RuntimeError(nat.lib().si_last_error().decode())
+        n += len(np.unique(t[t >= 0]))
+    return n * iterations
+
+
+def run_geodesic_bench(args, wl):
+    """Geodesic interpolation: value = volume voxels / geodesic_segment time
+    on device-resident inputs; e2e through geodesic_segment with numpy in/out;
+    roofline of the wavefront kernel over the whole scan."""
+    import torch
+
+    from biomedisa_gb300 import geodis as D
+    from biomedisa_gb300 import interpolation as I
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    img, lab = make_inputs("geodesic")
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    n_vox = int(np.prod(img.shape))
+    nol = len(np.unique(lab[lab >= 0]))
+    if args.impl == "reference":
+        if rank == 0:
+            import geo_oracle as G
+
+            times = []
+            for i in range(args.warmup + args.steps):
+                t0 = time.perf_counter()
+                G.geodesic_segment(img, lab)
+                if i >= args.warmup:
+                    times.append(time.perf_counter() - t0)
+            secs = statistics.median(times)
+            v = n_vox / secs
+            print(json.dumps({
+                "metric": "voxels/s", "value": v, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic", "impl": "reference",
+                "config": {"workload": wl["desc"], "global_batch": 1, "parallelism": "host cores"},
+                "cpu_baseline": {"value": v, "unit": "voxels/s", "cores": 1, "kind": "port",
+                                 "sample": "the whole volume; the reference's numba scan restated in C "
+                                           "(oracle/geo_oracle.c; numba is not installed), one core"},
+                "e2e": {"value": v, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    img_t, lab_t = I.upload(img, lab)
+    code_i, code_l = I._IMG_DTYPES[img.dtype], I._LAB_DTYPES[lab.dtype]
+    l2buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        D.geodesic_segment_device(img_t, code_i, lab_t, code_l)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    t_job, t_scan = [], []
+    # the scan alone, for the wavefront kernel's roofline (same inputs as a job)
+    work = torch.empty(img.shape, dtype=torch.float32, device="cuda")
+    mm = torch.empty(4, dtype=torch.int32, device="cuda")
+    from biomedisa_gb300 import _native as nat
+
+    nat.call("si_geo_normalize", img_t.data_ptr(), code_i, n_vox, work.data_ptr(), mm.data_ptr(),
+             stream.cuda_stream)
+    c0 = torch.full((nol,) + img.shape, float("inf"), dtype=torch.float32, device="cuda")
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            flush_l2(l2buf)
+            torch.cuda.synchronize()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record(stream)
+            D.geodesic_segment_device(img_t, code_i, lab_t, code_l)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            t_job.append(ev[0].elapsed_time(ev[1]))
+        for _ in range(args.steps):
+            c = c0.clone()
+            flush_l2(l2buf)
+            torch.cuda.synchronize()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record(stream)
+            D.scan_device(c, work)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            t_scan.append(ev[0].elapsed_time(ev[1]))
+    ms = sum(t_job) / len(t_job)
+    scan_ms = sum(t_scan) / len(t_scan)
+    D.geodesic_segment(img, lab)
+    t_e2e = []
+    for _ in range(args.steps):
+        flush_l2(l2buf)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = D.geodesic_segment(img, lab)
+        t_e2e.append(time.perf_counter() - t0)
+    e2e_s = sum(t_e2e) / len(t_e2e)
+    waves = geo_wave_launches(img.shape)
+    Z, Y, X = img.shape
+    updates = 4 * ((Z - 1) * (Y - 2) * (X - 2)) * 2 * nol  # voxel-label updates of one scan
+    bytes_alg = updates * (8 + 4 / nol)  # read + write the distance, the image shared by the labels
+    achieved = bytes_alg / (scan_ms / 1e3) / 1e9
+    pk = peaks()
+    hbm = float(pk.get("hbm_gbs", 6800.0))
+    line = {
+        "metric": "voxels/s", "value": n_vox / (ms / 1e3), "unit": "voxels/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded generator, no public dataset)",
+        "config": {"workload": wl["desc"], "global_batch": 1, "parallelism": "single GPU",
+                   "l2": "256 MiB buffer written before every timed step"},
+        "e2e": {"value": n_vox / e2e_s, "unit": "voxels/s", "seconds": e2e_s,
+                "h2d_bytes_per_step": int(img.nbytes + lab.nbytes), "d2h_bytes_per_step": int(r.nbytes)},
+        "gpu_launches": 3 + 1 + 1 + waves + 1,
+        "scan_ms": scan_ms, "wave_launches": waves, "us_per_wave_launch": scan_ms * 1e3 / waves,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None,
+                     "note": f"geo_wave_kernel over one scan ({waves} launches, {nol} labels per launch): "
+                             "algorithmic bytes = 8 B per voxel-label update (read + write the distance) + 4 B "
+                             "per voxel update (image) / CUDA-event scan duration; the scan is launch-bound "
+                             f"(one launch per wavefront x + 2y + 4z); peak {'measured' if pk else 'fallback'}"},
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        import geo_oracle as G
+
+        t0 = time.perf_counter()
+        G.geodesic_segment(img, lab)
+        secs = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n_vox / secs, "unit": "voxels/s", "cores": 1, "kind": "port",
+                                "sample": "the whole volume; the reference's numba scan restated in C "
+                                          "(oracle/geo_oracle.c), one core"}
+    print(json.dumps(line))
 
 
 def profile_jobs(args, wl):

@@ -77,6 +77,11 @@ _SIGNATURES = {
     "si_fill": [_c_void_p, _c_int, _c_int, _c_int, ctypes.c_double, _c_void_p, _c_int, _c_void_p, _c_u64, _c_void_p],
     "si_smooth_f32": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
     "si_smooth": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_geo_normalize": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_void_p, _c_void_p],
+    "si_geo_masks": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_int, _c_void_p, _c_void_p],
+    "si_geo_scan": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, ctypes.c_double, _c_int, _c_void_p],
+    "si_geo_select": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_void_p, _c_void_p],
+    "si_geo_visit_order": [_c_int, _c_int, _c_int, _c_int, _c_void_p],
 }
 
 EXPORTED = ("si_version", "si_last_error", *_SIGNATURES)

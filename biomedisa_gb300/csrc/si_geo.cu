@@ -1,0 +1,395 @@
+// Geodesic raster-scan interpolation (biomedisa/geodis.py): image
+// normalisation, per-label seed masks, the forward/backward raster scans and
+// the per-voxel label selection.
+//
+// The reference scan (geodis.py:44-76) is an in-place Gauss-Seidel sweep: a
+// voxel takes the minimum over itself and 13 neighbours that come EARLIER in
+// the pass's raster order. With t = x + 2y + 4z every one of the 13 forward
+// offsets lowers t (by 1..7) and every backward offset raises it, so all voxels
+// of one t read only finished values: one launch per wavefront t, in
+// increasing t (forward) or decreasing t (backward), reproduces the
+// sequential sweep exactly. All labels share each launch.
+//
+// Arithmetic (numba's typing of the reference, see the scan kernel): the
+// intensity difference and its square are binary32, the cost sum and the
+// comparison binary64, the store rounds to binary32.
+#include <cmath>
+
+#include "si_common.cuh"
+#include "si_internal.h"
+
+namespace si {
+namespace {
+
+// Forward offsets (dz, dy, dx) in the reference's order (geodis.py:12-26); the
+// backward scan uses their negations in the same order (:28-42).
+constexpr int kGeoOff[13][3] = {
+    {-1, -1, -1}, {-1, -1, 0}, {-1, -1, 1}, {-1, 0, -1}, {-1, 0, 0}, {-1, 0, 1}, {-1, 1, -1},
+    {-1, 1, 0},   {-1, 1, 1},  {0, -1, -1}, {0, -1, 0},  {0, -1, 1}, {0, 0, -1},
+};
+
+__host__ __device__ inline int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+__host__ __device__ inline int ceil_div(int a, int b) { return -floor_div(-a, b); }
+__host__ __device__ inline int imax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ inline int imin(int a, int b) { return a < b ? a : b; }
+
+// The voxels of wavefront t: x = t - 2y - 4z inside the pass's domain
+// (forward z = 1..Z-1, backward z = 0..Z-2; both y = 1..Y-2, x = 1..X-2).
+// Thread (zi, j) of a launch takes z = zlo + zi (zi < nz) and the j-th valid y
+// of that plane (j < jmax = the most y values any plane can have).
+struct GeoWave {
+  int t, zlo, nz, jmax;
+};
+
+__host__ __device__ inline GeoWave geo_wave(int Z, int Y, int X, int fwd, int t) {
+  GeoWave w{t, 0, 0, (X - 1) / 2};
+  const int zmin = fwd ? 1 : 0, zmax = fwd ? Z - 1 : Z - 2;
+  // 1 <= x = t - 2y - 4z <= X-2 and 1 <= y <= Y-2 bound 4z to [t-(X-2)-2(Y-2), t-3]
+  const int zlo = imax(zmin, ceil_div(t - (X - 2) - 2 * (Y - 2), 4));
+  const int zhi = imin(zmax, floor_div(t - 3, 4));
+  w.zlo = zlo;
+  w.nz = zhi >= zlo ? zhi - zlo + 1 : 0;
+  return w;
+}
+
+__host__ __device__ inline bool geo_wave_voxel(int Y, int X, const GeoWave& w, int zi, int j, int* z, int* y,
+                                               int* x) {
+  const int zz = w.zlo + zi;
+  const int r = w.t - 4 * zz;
+  const int ylo = imax(1, ceil_div(r - (X - 2), 2));
+  const int yhi = imin(Y - 2, floor_div(r - 1, 2));
+  const int yy = ylo + j;
+  if (yy > yhi) return false;
+  *z = zz;
+  *y = yy;
+  *x = r - 2 * yy;
+  return true;
+}
+
+// Wavefront ranges of one pass: first, last (inclusive) and step.
+inline void geo_t_range(int Z, int Y, int X, int fwd, int* t0, int* t1, int* step) {
+  if (fwd) {
+    *t0 = 1 + 2 + 4;
+    *t1 = (X - 2) + 2 * (Y - 2) + 4 * (Z - 1);
+    *step = 1;
+  } else {
+    *t0 = (X - 2) + 2 * (Y - 2) + 4 * (Z - 2);
+    *t1 = 1 + 2 + 0;
+    *step = -1;
+  }
+}
+
+inline bool geo_has_interior(int Z, int Y, int X) { return Z >= 2 && Y >= 3 && X >= 3; }
+
+struct GeoScanArgs {
+  float* c;
+  const float* img;
+  int Z, Y, X, nol;
+  long long V;
+  long long off[13];  // forward linear offsets
+  double w[13];       // (1 - lamb) * |offset|
+  double lamb;
+};
+
+// One wavefront for all labels. kLamb1: lamb == 1.0, where the reference's
+// float64 cost c[q] + 0.0 + 1.0*sq equals the binary64 sum of two binary32
+// values; rounding that sum to binary32 equals the binary32 sum (double
+// rounding is innocuous for addition when 53 >= 2*24 + 2), and rounding is
+// monotone, so the stored minimum is the binary32 minimum of the binary32
+// sums. Otherwise the float64 expression is evaluated as written.
+template <bool kLamb1>
+__global__ void __launch_bounds__(256) geo_wave_kernel(GeoScanArgs a, GeoWave w, int fwd) {
+  const long long per_label = (long long)w.nz * w.jmax;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= per_label * a.nol) return;
+  const int k = (int)(i / per_label);
+  const long long r = i - (long long)k * per_label;
+  const int zi = (int)(r / w.jmax);
+  const int j = (int)(r - (long long)zi * w.jmax);
+  int z, y, x;
+  if (!geo_wave_voxel(a.Y, a.X, w, zi, j, &z, &y, &x)) return;
+  const long long v = ((long long)z * a.Y + y) * a.X + x;
+  float* cl = a.c + (long long)k * a.V;
+  const float iv = a.img[v];
+  if (kLamb1) {
+    float best = cl[v];
+#pragma unroll
+    for (int n = 0; n < 13; ++n) {
+      const long long q = fwd ? v + a.off[n] : v - a.off[n];
+      const float diff = __fsub_rn(iv, a.img[q]);
+      const float cost = __fadd_rn(cl[q], __fmul_rn(diff, diff));
+      if (cost < best) best = cost;
+    }
+    cl[v] = best;
+  } else {
+    double best = (double)cl[v];
+#pragma unroll
+    for (int n = 0; n < 13; ++n) {
+      const long long q = fwd ? v + a.off[n] : v - a.off[n];
+      const float diff = __fsub_rn(iv, a.img[q]);
+      const double sq = (double)__fmul_rn(diff, diff);
+      const double cost = __dadd_rn(__dadd_rn((double)cl[q], a.w[n]), __dmul_rn(a.lamb, sq));
+      if (cost < best) best = cost;
+    }
+    cl[v] = __double2float_rn(best);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Normalisation (geodis.py:86-88): image.astype(float32); image -= amin;
+// image /= amax. amin/amax follow numpy: a NaN anywhere makes them NaN.
+// Rounding is monotone, so amax of (image - amin) is fl(max - amin).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t ord_key(float f) {
+  const uint32_t b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__device__ __forceinline__ float ord_value(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+template <typename T>
+__device__ __forceinline__ float to_f32(T v) {
+  return (float)v;  // exact for 8/16-bit integers and float
+}
+template <>
+__device__ __forceinline__ float to_f32<int32_t>(int32_t v) {
+  return __int2float_rn(v);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) geo_convert_minmax_kernel(const T* __restrict__ img, uint64_t n,
+                                                                 float* __restrict__ out, uint32_t* mm) {
+  uint32_t lo = 0xffffffffu, hi = 0u, nan = 0u;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float f = to_f32(img[i]);
+    out[i] = f;
+    if (f != f) {
+      nan = 1u;
+    } else {
+      const uint32_t k = ord_key(f);
+      lo = k < lo ? k : lo;
+      hi = k > hi ? k : hi;
+    }
+  }
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  nan = __reduce_or_sync(0xffffffffu, nan);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&mm[0], lo);
+    atomicMax(&mm[1], hi);
+    if (nan) atomicOr(&mm[2], 1u);
+  }
+}
+
+__global__ void geo_minmax_init_kernel(uint32_t* mm) {
+  if (threadIdx.x == 0) {
+    mm[0] = 0xffffffffu;
+    mm[1] = 0u;
+    mm[2] = 0u;
+  }
+}
+
+__global__ void __launch_bounds__(256) geo_normalize_kernel(float* __restrict__ out, uint64_t n,
+                                                            const uint32_t* __restrict__ mm) {
+  float mn = ord_value(mm[0]);
+  float amax = __fsub_rn(ord_value(mm[1]), mn);
+  // numpy: NaN in the image, or an infinite minimum (inf - inf inside image - amin), gives NaN everywhere
+  if (mm[2] || isinf(mn)) {
+    mn = __uint_as_float(0x7fffffffu);
+    amax = mn;
+  }
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    out[i] = __fdiv_rn(__fsub_rn(out[i], mn), amax);
+}
+
+// mask.fill(inf); mask[labels == label] = 0 for every label slot at once
+// (geodis.py:95-96). slot_lut[v] = slot of label value v (0..255) or -1.
+template <typename T>
+__global__ void __launch_bounds__(256) geo_masks_kernel(const T* __restrict__ lab, uint64_t n,
+                                                        const int16_t* __restrict__ slot_lut, int nol,
+                                                        float* __restrict__ c) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int v = (int)lab[i];
+    const int s = (v >= 0 && v <= 255) ? (int)slot_lut[v] : -1;
+    for (int k = 0; k < nol; ++k) c[(uint64_t)k * n + i] = (s == k) ? 0.0f : __uint_as_float(0x7f800000u);
+  }
+}
+
+// The label loop of geodis.py:94-103: slot 0 only initialises the running
+// minimum (its voxels keep result 0); a later slot wins where its distance is
+// strictly smaller.
+__global__ void __launch_bounds__(256) geo_select_kernel(const float* __restrict__ c, int nol, uint64_t n,
+                                                         const uint8_t* __restrict__ slot_label,
+                                                         uint8_t* __restrict__ out) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    float m = c[i];
+    uint8_t r = 0;
+    for (int k = 1; k < nol; ++k) {
+      const float d = c[(uint64_t)k * n + i];
+      if (d < m) {
+        m = d;
+        r = slot_label[k];
+      }
+    }
+    out[i] = r;
+  }
+}
+
+inline int grid_for(uint64_t n, int block) {
+  const uint64_t want = (n + block - 1) / block;
+  const uint64_t cap = (uint64_t)sm_count() * 16;
+  return (int)(want < cap ? (want > 0 ? want : 1) : cap);
+}
+
+}  // namespace
+}  // namespace si
+
+using namespace si;
+
+extern "C" int si_geo_normalize(const void* img, int dtype, uint64_t n, float* out, uint32_t* mm, void* stream) {
+  clear_error();
+  if (!img || !out || !mm) return set_error(SI_ERR_ARG, "si_geo_normalize: null pointer");
+  if (n == 0) return set_error(SI_ERR_ARG, "si_geo_normalize: empty image (numpy's amin has no identity)");
+  if (dtype_size(dtype) == 0) return set_error(SI_ERR_ARG, "si_geo_normalize: unsupported image dtype %d", dtype);
+  cudaStream_t st = as_stream(stream);
+  geo_minmax_init_kernel<<<1, 32, 0, st>>>(mm);
+  const int block = 256, grid = grid_for(n, block);
+  switch (dtype) {
+    case SI_U8:
+      geo_convert_minmax_kernel<<<grid, block, 0, st>>>(static_cast<const uint8_t*>(img), n, out, mm);
+      break;
+    case SI_I8:
+      geo_convert_minmax_kernel<<<grid, block, 0, st>>>(static_cast<const int8_t*>(img), n, out, mm);
+      break;
+    case SI_U16:
+      geo_convert_minmax_kernel<<<grid, block, 0, st>>>(static_cast<const uint16_t*>(img), n, out, mm);
+      break;
+    case SI_I16:
+      geo_convert_minmax_kernel<<<grid, block, 0, st>>>(static_cast<const int16_t*>(img), n, out, mm);
+      break;
+    case SI_I32:
+      geo_convert_minmax_kernel<<<grid, block, 0, st>>>(static_cast<const int32_t*>(img), n, out, mm);
+      break;
+    case SI_F32:
+      geo_convert_minmax_kernel<<<grid, block, 0, st>>>(static_cast<const float*>(img), n, out, mm);
+      break;
+    default:
+      return set_error(SI_ERR_ARG, "si_geo_normalize: unsupported image dtype %d", dtype);
+  }
+  geo_normalize_kernel<<<grid, block, 0, st>>>(out, n, mm);
+  return check_launch("si_geo_normalize");
+}
+
+extern "C" int si_geo_masks(const void* labels, int dtype, uint64_t n, const int16_t* slot_lut, int nol, float* c,
+                            void* stream) {
+  clear_error();
+  if (!labels || !slot_lut || !c) return set_error(SI_ERR_ARG, "si_geo_masks: null pointer");
+  if (nol < 1 || nol > 256) return set_error(SI_ERR_ARG, "si_geo_masks: nol must be 1..256");
+  if (n == 0) return SI_OK;
+  const int block = 256, grid = grid_for(n, block);
+  cudaStream_t st = as_stream(stream);
+  switch (dtype) {
+    case SI_U8:
+      geo_masks_kernel<<<grid, block, 0, st>>>(static_cast<const uint8_t*>(labels), n, slot_lut, nol, c);
+      break;
+    case SI_I16:
+      geo_masks_kernel<<<grid, block, 0, st>>>(static_cast<const int16_t*>(labels), n, slot_lut, nol, c);
+      break;
+    case SI_I32:
+      geo_masks_kernel<<<grid, block, 0, st>>>(static_cast<const int32_t*>(labels), n, slot_lut, nol, c);
+      break;
+    default:
+      return set_error(SI_ERR_ARG, "si_geo_masks: unsupported label dtype %d", dtype);
+  }
+  return check_launch("si_geo_masks");
+}
+
+extern "C" int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int nol, double lamb, int iterations,
+                           void* stream) {
+  clear_error();
+  if (!c || !img) return set_error(SI_ERR_ARG, "si_geo_scan: null pointer");
+  if (Z < 1 || Y < 1 || X < 1 || nol < 1 || iterations < 0) return set_error(SI_ERR_ARG, "si_geo_scan: bad arguments");
+  if ((long long)X + 2LL * Y + 4LL * Z > 0x7fffffffLL) return set_error(SI_ERR_LIMIT, "si_geo_scan: volume too large");
+  if (!geo_has_interior(Z, Y, X) || iterations == 0) return SI_OK;
+  GeoScanArgs a{};
+  a.c = c;
+  a.img = img;
+  a.Z = Z;
+  a.Y = Y;
+  a.X = X;
+  a.nol = nol;
+  a.V = (long long)Z * Y * X;
+  a.lamb = lamb;
+  const long long YX = (long long)Y * X;
+  for (int n = 0; n < 13; ++n) {
+    a.off[n] = kGeoOff[n][0] * YX + (long long)kGeoOff[n][1] * X + kGeoOff[n][2];
+    const int nzc = (kGeoOff[n][0] != 0) + (kGeoOff[n][1] != 0) + (kGeoOff[n][2] != 0);
+    const double d = nzc == 3 ? std::sqrt(3.0) : nzc == 2 ? std::sqrt(2.0) : 1.0;
+    a.w[n] = (1.0 - lamb) * d;
+  }
+  const bool lamb1 = (lamb == 1.0);
+  cudaStream_t st = as_stream(stream);
+  const int block = 256;
+  for (int it = 0; it < iterations; ++it) {
+    for (int fwd = 1; fwd >= 0; --fwd) {
+      int t0, t1, step;
+      geo_t_range(Z, Y, X, fwd, &t0, &t1, &step);
+      for (int t = t0; step > 0 ? t <= t1 : t >= t1; t += step) {
+        const GeoWave w = geo_wave(Z, Y, X, fwd, t);
+        if (w.nz == 0) continue;
+        const long long threads = (long long)w.nz * w.jmax * nol;
+        const long long blocks = (threads + block - 1) / block;
+        if (blocks > 0x7fffffffLL) return set_error(SI_ERR_LIMIT, "si_geo_scan: wavefront too large");
+        if (lamb1)
+          geo_wave_kernel<true><<<(unsigned)blocks, block, 0, st>>>(a, w, fwd);
+        else
+          geo_wave_kernel<false><<<(unsigned)blocks, block, 0, st>>>(a, w, fwd);
+      }
+    }
+    const int rc = check_launch("si_geo_scan");
+    if (rc) return rc;
+  }
+  return SI_OK;
+}
+
+extern "C" int si_geo_select(const float* c, int nol, uint64_t n, const uint8_t* slot_label, uint8_t* out,
+                             void* stream) {
+  clear_error();
+  if (!c || !slot_label || !out) return set_error(SI_ERR_ARG, "si_geo_select: null pointer");
+  if (nol < 1 || nol > 256) return set_error(SI_ERR_ARG, "si_geo_select: nol must be 1..256");
+  if (n == 0) return SI_OK;
+  const int block = 256, grid = grid_for(n, block);
+  geo_select_kernel<<<grid, block, 0, as_stream(stream)>>>(c, nol, n, slot_label, out);
+  return check_launch("si_geo_select");
+}
+
+extern "C" int si_geo_visit_order(int Z, int Y, int X, int fwd, int32_t* t_of_voxel) {
+  clear_error();
+  if (!t_of_voxel || Z < 1 || Y < 1 || X < 1) return set_error(SI_ERR_ARG, "si_geo_visit_order: bad arguments");
+  const long long V = (long long)Z * Y * X;
+  for (long long v = 0; v < V; ++v) t_of_voxel[v] = -1;
+  if (!geo_has_interior(Z, Y, X)) return SI_OK;
+  int t0, t1, step;
+  geo_t_range(Z, Y, X, fwd ? 1 : 0, &t0, &t1, &step);
+  for (int t = t0; step > 0 ? t <= t1 : t >= t1; t += step) {
+    const GeoWave w = geo_wave(Z, Y, X, fwd ? 1 : 0, t);
+    for (int zi = 0; zi < w.nz; ++zi)
+      for (int j = 0; j < w.jmax; ++j) {
+        int z, y, x;
+        if (!geo_wave_voxel(Y, X, w, zi, j, &z, &y, &x)) continue;
+        if (z < 0 || z >= Z || y < 0 || y >= Y || x < 0 || x >= X)
+          return set_error(SI_ERR_LIMIT, "si_geo_visit_order: voxel (%d,%d,%d) outside the volume", z, y, x);
+        const long long v = ((long long)z * Y + y) * X + x;
+        if (t_of_voxel[v] != -1)
+          return set_error(SI_ERR_LIMIT, "si_geo_visit_order: voxel (%d,%d,%d) visited twice", z, y, x);
+        t_of_voxel[v] = t;
+      }
+  }
+  return SI_OK;
+}

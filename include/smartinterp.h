@@ -333,6 +333,47 @@ int si_fill(uint8_t* img, int Z, int Y, int X, double threshold,
             const int* label_list, int n_labels, void* scratch,
             uint64_t scratch_bytes, void* stream);
 
+/* ---- geodesic raster-scan interpolation (biomedisa/geodis.py) ----
+ * The sequence geodesic_segment() runs is:
+ *   si_geo_normalize -> si_label_histogram -> (host: label slots)
+ *   -> si_geo_masks -> si_geo_scan -> si_geo_select */
+
+/* out = normalised float32 image: x = float32(img); x -= min(x); x /= max(x)
+ * (geodis.py:86-88, numpy semantics: a NaN or an infinite minimum gives NaN
+ * everywhere, a constant image 0/0 = NaN). mm: 3 uint32 of device scratch
+ * (min/max keys and a NaN flag), overwritten. n >= 1.
+ * dtype: SI_U8, SI_I8, SI_U16, SI_I16, SI_I32 or SI_F32. */
+int si_geo_normalize(const void* img, int dtype, uint64_t n, float* out,
+                     uint32_t* mm, void* stream);
+
+/* Distance seeds of every label slot at once: c[k][v] = 0 where the label
+ * value of voxel v has slot k, +inf elsewhere (geodis.py:95-96).
+ * slot_lut[v] = slot of label value v (0..255) or -1; values outside 0..255
+ * have no slot. c: float32 [nol][n]. dtype: SI_U8, SI_I16 or SI_I32. */
+int si_geo_masks(const void* labels, int dtype, uint64_t n,
+                 const int16_t* slot_lut, int nol, float* c, void* stream);
+
+/* Replaces geodesic_raster_scan (geodis.py:44-76), run on nol distance
+ * volumes c[nol][Z][Y][X] (float32, updated in place) over one float32 image
+ * img[Z][Y][X]: `iterations` times a forward and a backward raster pass with
+ * cost c[q] + (1 - lamb)|q - p| + lamb (img[p] - img[q])^2, results identical
+ * to the sequential scan. One kernel launch per wavefront x + 2y + 4z (about
+ * X + 2Y + 4Z per pass), all volumes in each launch. */
+int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int nol,
+                double lamb, int iterations, void* stream);
+
+/* out[v] = slot_label[k] of the first slot k >= 1 whose distance is strictly
+ * below the running minimum that starts at slot 0's, else 0 (the label loop of
+ * geodesic_segment, geodis.py:94-103). */
+int si_geo_select(const float* c, int nol, uint64_t n,
+                  const uint8_t* slot_label, uint8_t* out, void* stream);
+
+/* Host only (no device work): t_of_voxel[v] = the wavefront at which
+ * si_geo_scan's forward (fwd = 1) or backward (fwd = 0) pass updates voxel v,
+ * -1 for voxels the pass leaves alone. Fails if a voxel would be updated
+ * twice. The launch plan of si_geo_scan, exposed for checking its order. */
+int si_geo_visit_order(int Z, int Y, int X, int fwd, int32_t* t_of_voxel);
+
 /* ---- learned surrogate (no counterpart in the reference) ----
  * Tensors are NDHWC; activations bfloat16, weights bfloat16 [27][cout][cin]
  * (tap-major, tap = (dz+1)*9 + (dy+1)*3 + (dx+1)), biases and gradients fp32.

@@ -57,15 +57,102 @@ class _Program:
         return _AnyCallable()
 
 
+class _NumbaF32:
+    """A float32 scalar read from a float32 array inside a numba-compiled
+    function, with numba's typing of the operations geodesic_raster_scan
+    (geodis.py:44-76) applies to it:
+      float32 - float32  -> float32 (binary32 subtraction)
+      float32 ** int     -> float32 (repeated binary32 multiplication, as
+                            numba's integer power does)
+      float32 + float64, float64 * float32 -> float64
+      comparisons        -> on the exact values.
+    Plain NumPy-2 scalars differ: a Python float added to an np.float32 stays
+    float32 there (NEP 50), where numba computes in float64."""
+
+    __slots__ = ("v",)
+
+    def __init__(self, v):
+        import numpy as np
+
+        self.v = np.float32(v)
+
+    def __sub__(self, o):
+        return _NumbaF32(self.v - o.v)
+
+    def __pow__(self, k):
+        import numpy as np
+
+        if not isinstance(k, int) or k < 0:
+            raise TypeError("only non-negative integer powers are emulated")
+        r, a = np.float32(1.0), self.v
+        while True:
+            if k & 1:
+                r = np.float32(r * a)
+            k >>= 1
+            if not k:
+                return _NumbaF32(r)
+            a = np.float32(a * a)
+
+    def __add__(self, o):
+        return float(self.v) + float(o)
+
+    __radd__ = __add__
+
+    def __rmul__(self, o):
+        return float(o) * float(self.v)
+
+    def __float__(self):
+        return float(self.v)
+
+    def __lt__(self, o):
+        return float(self.v) < float(o)
+
+    def __gt__(self, o):
+        return float(self.v) > float(o)
+
+
+class _NumbaF32Array:
+    """View of a float32 array whose reads give _NumbaF32 scalars and whose
+    stores round a float64 value to float32, as numba's setitem does."""
+
+    def __init__(self, a):
+        self.a = a
+        self.shape = a.shape
+
+    def __getitem__(self, idx):
+        return _NumbaF32(self.a[idx])
+
+    def __setitem__(self, idx, value):
+        import numpy as np
+
+        self.a[idx] = np.float32(float(value))
+
+
 def _numba_typed(f):
     """Runs a numba-compiled function as Python with numba's scalar typing
-    where plain Python/NumPy-2 typing differs: smooth_img_3x3
-    (biomedisa_helper.py:308-323) starts its accumulator at the integer 0,
-    which numba types as int64 (float64 once a float is added); under NumPy 2
-    rules a Python 0 plus a uint8 scalar stays uint8 and overflows. The input
-    is widened to int64/float64 for the call and the result cast back to the
-    input dtype, as numba's store into the uint8/float32 output does."""
-    if getattr(f, "__name__", "") != "smooth_img_3x3":
+    where plain Python/NumPy-2 typing differs.
+    smooth_img_3x3 (biomedisa_helper.py:308-323) starts its accumulator at the
+    integer 0, which numba types as int64 (float64 once a float is added);
+    under NumPy 2 rules a Python 0 plus a uint8 scalar stays uint8 and
+    overflows. The input is widened to int64/float64 for the call and the
+    result cast back to the input dtype, as numba's store into the
+    uint8/float32 output does.
+    geodesic_raster_scan (geodis.py:44-76) runs on float32 views that follow
+    numba's float32/float64 typing (_NumbaF32)."""
+    name = getattr(f, "__name__", "")
+    if name == "geodesic_raster_scan":
+
+        def scan(img, c, lamb=1.0, iterations=4):
+            import numpy as np
+
+            if img.dtype != np.float32 or c.dtype != np.float32:
+                raise TypeError("the typed emulation covers float32 img and c only")
+            f(_NumbaF32Array(img), _NumbaF32Array(c), lamb, iterations)
+            return c
+
+        scan.__name__ = name
+        return scan
+    if name != "smooth_img_3x3":
         return f
 
     def wrapper(img):
