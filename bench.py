@@ -824,22 +824,6 @@ def run_hybrid_bench(args, wl):
         print(json.dumps(line))
 
 
-def geo_wave_launches(shape, iterations=4):
-    """Wavefront launches of one si_geo_scan call (both passes, all iterations),
-    from the library's own launch plan."""
-    import ctypes
-
-    from biomedisa_gb300 import _native as nat
-
-    n = 0
-    t = np.empty(shape, np.int32)
-    for fwd in (1, 0):
-        if nat.lib().si_geo_visit_order(*shape, fwd, t.ctypes.data_as(ctypes.c_void_p)) != 0:
-            raise RuntimeError(nat.lib().si_last_error().decode())
-        n += len(np.unique(t[t >= 0]))
-    return n * iterations
-
-
 def run_geodesic_bench(args, wl):
     """Geodesic interpolation: value = volume voxels / geodesic_segment time
     on device-resident inputs; e2e through geodesic_segment with numpy in/out;
@@ -893,6 +877,8 @@ def run_geodesic_bench(args, wl):
     nat.call("si_geo_normalize", img_t.data_ptr(), code_i, n_vox, work.data_ptr(), mm.data_ptr(),
              stream.cuda_stream)
     c0 = torch.full((nol,) + img.shape, float("inf"), dtype=torch.float32, device="cuda")
+    c0[:, ::9, ::11, ::13] = 0.0
+    scan_ms_mode = {}
     with ClockSampler(0) as clocks:
         for _ in range(args.steps):
             flush_l2(l2buf)
@@ -903,18 +889,21 @@ def run_geodesic_bench(args, wl):
             ev[1].record(stream)
             torch.cuda.synchronize()
             t_job.append(ev[0].elapsed_time(ev[1]))
-        for _ in range(args.steps):
-            c = c0.clone()
-            flush_l2(l2buf)
-            torch.cuda.synchronize()
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-            ev[0].record(stream)
-            D.scan_device(c, work)
-            ev[1].record(stream)
-            torch.cuda.synchronize()
-            t_scan.append(ev[0].elapsed_time(ev[1]))
+        for mode in (D.SCAN_AUTO, D.SCAN_WAVEFRONTS, D.SCAN_CLUSTER):
+            t_scan = []
+            for _ in range(args.steps):
+                c = c0.clone()
+                flush_l2(l2buf)
+                torch.cuda.synchronize()
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                ev[0].record(stream)
+                D.scan_device(c, work, mode=mode)
+                ev[1].record(stream)
+                torch.cuda.synchronize()
+                t_scan.append(ev[0].elapsed_time(ev[1]))
+            scan_ms_mode[mode] = sum(t_scan) / len(t_scan)
     ms = sum(t_job) / len(t_job)
-    scan_ms = sum(t_scan) / len(t_scan)
+    scan_ms = scan_ms_mode[D.SCAN_AUTO]
     D.geodesic_segment(img, lab)
     t_e2e = []
     for _ in range(args.steps):
@@ -924,7 +913,8 @@ def run_geodesic_bench(args, wl):
         r = D.geodesic_segment(img, lab)
         t_e2e.append(time.perf_counter() - t0)
     e2e_s = sum(t_e2e) / len(t_e2e)
-    waves = geo_wave_launches(img.shape)
+    scan_launches = D.scan_launches(img.shape)
+    waves = D.scan_launches(img.shape, mode=D.SCAN_WAVEFRONTS)
     Z, Y, X = img.shape
     updates = 4 * ((Z - 1) * (Y - 2) * (X - 2)) * 2 * nol  # voxel-label updates of one scan
     bytes_alg = updates * (8 + 4 / nol)  # read + write the distance, the image shared by the labels
@@ -939,14 +929,17 @@ def run_geodesic_bench(args, wl):
                    "l2": "256 MiB buffer written before every timed step"},
         "e2e": {"value": n_vox / e2e_s, "unit": "voxels/s", "seconds": e2e_s,
                 "h2d_bytes_per_step": int(img.nbytes + lab.nbytes), "d2h_bytes_per_step": int(r.nbytes)},
-        "gpu_launches": 3 + 1 + 1 + waves + 1,
-        "scan_ms": scan_ms, "wave_launches": waves, "us_per_wave_launch": scan_ms * 1e3 / waves,
+        "gpu_launches": 3 + 1 + 1 + scan_launches + 1,
+        "scan_ms": scan_ms, "scan_mode": "cluster" if scan_launches == 1 else "wavefronts",
+        "scan_ms_wavefronts": scan_ms_mode[D.SCAN_WAVEFRONTS], "scan_ms_cluster": scan_ms_mode[D.SCAN_CLUSTER],
+        "wavefronts_per_scan": waves, "us_per_wavefront": scan_ms * 1e3 / waves,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": None,
-                     "note": f"geo_wave_kernel over one scan ({waves} launches, {nol} labels per launch): "
-                             "algorithmic bytes = 8 B per voxel-label update (read + write the distance) + 4 B "
-                             "per voxel update (image) / CUDA-event scan duration; the scan is launch-bound "
-                             f"(one launch per wavefront x + 2y + 4z); peak {'measured' if pk else 'fallback'}"},
+                     "note": f"the scan kernel over one scan ({scan_launches} launch(es), {waves} wavefronts, "
+                             f"{nol} labels): algorithmic bytes = 8 B per voxel-label update (read + write the "
+                             "distance) + 4 B per voxel update (image) / CUDA-event scan duration; latency-bound: "
+                             "the wavefronts x + 2y + 4z run one after another; peak "
+                             f"{'measured' if pk else 'fallback'} HBM"},
         "clocks": clocks.summary(),
     }
     if not args.no_cpu_baseline:

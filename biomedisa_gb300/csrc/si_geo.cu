@@ -67,7 +67,7 @@ __host__ __device__ inline bool geo_wave_voxel(int Y, int X, const GeoWave& w, i
 }
 
 // Wavefront ranges of one pass: first, last (inclusive) and step.
-inline void geo_t_range(int Z, int Y, int X, int fwd, int* t0, int* t1, int* step) {
+__host__ __device__ inline void geo_t_range(int Z, int Y, int X, int fwd, int* t0, int* t1, int* step) {
   if (fwd) {
     *t0 = 1 + 2 + 4;
     *t1 = (X - 2) + 2 * (Y - 2) + 4 * (Z - 1);
@@ -91,12 +91,44 @@ struct GeoScanArgs {
   double lamb;
 };
 
-// One wavefront for all labels. kLamb1: lamb == 1.0, where the reference's
-// float64 cost c[q] + 0.0 + 1.0*sq equals the binary64 sum of two binary32
-// values; rounding that sum to binary32 equals the binary32 sum (double
-// rounding is innocuous for addition when 53 >= 2*24 + 2), and rounding is
-// monotone, so the stored minimum is the binary32 minimum of the binary32
-// sums. Otherwise the float64 expression is evaluated as written.
+// Update of voxel v of one distance map cl. kLamb1: lamb == 1.0, where the
+// reference's float64 cost c[q] + 0.0 + 1.0*sq equals the binary64 sum of two
+// binary32 values; rounding that sum to binary32 equals the binary32 sum
+// (double rounding is innocuous for addition when 53 >= 2*24 + 2), and
+// rounding is monotone, so the stored minimum is the binary32 minimum of the
+// binary32 sums. Otherwise the float64 expression is evaluated as written.
+// kL2: distance loads bypass L1 (ld.global.cg), for the cluster scan whose
+// CTAs exchange values through L2 inside one launch.
+template <bool kLamb1, bool kL2>
+__device__ __forceinline__ void geo_update(const GeoScanArgs& a, float* cl, long long v, int fwd) {
+  const float iv = a.img[v];
+  if (kLamb1) {
+    float best = kL2 ? __ldcg(cl + v) : cl[v];
+#pragma unroll
+    for (int n = 0; n < 13; ++n) {
+      const long long q = fwd ? v + a.off[n] : v - a.off[n];
+      const float diff = __fsub_rn(iv, a.img[q]);
+      const float cq = kL2 ? __ldcg(cl + q) : cl[q];
+      const float cost = __fadd_rn(cq, __fmul_rn(diff, diff));
+      if (cost < best) best = cost;
+    }
+    cl[v] = best;
+  } else {
+    double best = (double)(kL2 ? __ldcg(cl + v) : cl[v]);
+#pragma unroll
+    for (int n = 0; n < 13; ++n) {
+      const long long q = fwd ? v + a.off[n] : v - a.off[n];
+      const float diff = __fsub_rn(iv, a.img[q]);
+      const double sq = (double)__fmul_rn(diff, diff);
+      const float cq = kL2 ? __ldcg(cl + q) : cl[q];
+      const double cost = __dadd_rn(__dadd_rn((double)cq, a.w[n]), __dmul_rn(a.lamb, sq));
+      if (cost < best) best = cost;
+    }
+    cl[v] = __double2float_rn(best);
+  }
+}
+
+// Wavefront mode: one launch per wavefront t, one thread per (label, voxel).
 template <bool kLamb1>
 __global__ void __launch_bounds__(256) geo_wave_kernel(GeoScanArgs a, GeoWave w, int fwd) {
   const long long per_label = (long long)w.nz * w.jmax;
@@ -108,30 +140,44 @@ __global__ void __launch_bounds__(256) geo_wave_kernel(GeoScanArgs a, GeoWave w,
   const int j = (int)(r - (long long)zi * w.jmax);
   int z, y, x;
   if (!geo_wave_voxel(a.Y, a.X, w, zi, j, &z, &y, &x)) return;
-  const long long v = ((long long)z * a.Y + y) * a.X + x;
+  geo_update<kLamb1, false>(a, a.c + (long long)k * a.V, ((long long)z * a.Y + y) * a.X + x, fwd);
+}
+
+// Cluster mode: one thread-block cluster of kGeoCluster CTAs per label runs
+// every pass and wavefront of the scan in one launch; the cluster's hardware
+// barrier (release/acquire at cluster scope) separates the wavefronts. Every
+// thread runs the same loop bounds (they depend on t only) and reaches every
+// barrier; no thread leaves early.
+constexpr int kGeoCluster = 8;
+constexpr int kGeoClusterThreads = 1024;
+
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+template <bool kLamb1>
+__global__ void __launch_bounds__(kGeoClusterThreads, 1) geo_cluster_scan_kernel(GeoScanArgs a, int iterations) {
+  const int k = blockIdx.x / kGeoCluster;
+  const int tid = (blockIdx.x % kGeoCluster) * kGeoClusterThreads + threadIdx.x;
+  const int nthr = kGeoCluster * kGeoClusterThreads;
   float* cl = a.c + (long long)k * a.V;
-  const float iv = a.img[v];
-  if (kLamb1) {
-    float best = cl[v];
-#pragma unroll
-    for (int n = 0; n < 13; ++n) {
-      const long long q = fwd ? v + a.off[n] : v - a.off[n];
-      const float diff = __fsub_rn(iv, a.img[q]);
-      const float cost = __fadd_rn(cl[q], __fmul_rn(diff, diff));
-      if (cost < best) best = cost;
+  for (int it = 0; it < iterations; ++it) {
+    for (int fwd = 1; fwd >= 0; --fwd) {
+      int t0, t1, step;
+      geo_t_range(a.Z, a.Y, a.X, fwd, &t0, &t1, &step);
+      for (int t = t0; step > 0 ? t <= t1 : t >= t1; t += step) {
+        const GeoWave w = geo_wave(a.Z, a.Y, a.X, fwd, t);
+        if (w.nz == 0) continue;  // uniform across the cluster
+        const int per = w.nz * w.jmax;
+        for (int i = tid; i < per; i += nthr) {
+          const int zi = i / w.jmax, j = i - zi * w.jmax;
+          int z, y, x;
+          if (geo_wave_voxel(a.Y, a.X, w, zi, j, &z, &y, &x))
+            geo_update<kLamb1, true>(a, cl, ((long long)z * a.Y + y) * a.X + x, fwd);
+        }
+        cluster_barrier();
+      }
     }
-    cl[v] = best;
-  } else {
-    double best = (double)cl[v];
-#pragma unroll
-    for (int n = 0; n < 13; ++n) {
-      const long long q = fwd ? v + a.off[n] : v - a.off[n];
-      const float diff = __fsub_rn(iv, a.img[q]);
-      const double sq = (double)__fmul_rn(diff, diff);
-      const double cost = __dadd_rn(__dadd_rn((double)cl[q], a.w[n]), __dmul_rn(a.lamb, sq));
-      if (cost < best) best = cost;
-    }
-    cl[v] = __double2float_rn(best);
   }
 }
 
@@ -310,11 +356,102 @@ extern "C" int si_geo_masks(const void* labels, int dtype, uint64_t n, const int
   return check_launch("si_geo_masks");
 }
 
+namespace si {
+namespace {
+
+// Clusters of the scan kernel that fit on the current device at once (0 if
+// the cluster launch is not possible), cached per device.
+int geo_cluster_capacity(bool lamb1) {
+  static int cache[2][64];
+  static bool known[2][64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  if (known[lamb1][dev]) return cache[lamb1][dev];
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kGeoCluster);
+  cfg.blockDim = dim3(kGeoClusterThreads);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kGeoCluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  const cudaError_t e =
+      lamb1 ? cudaOccupancyMaxActiveClusters(&n, geo_cluster_scan_kernel<true>, &cfg)
+            : cudaOccupancyMaxActiveClusters(&n, geo_cluster_scan_kernel<false>, &cfg);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    n = 0;
+  }
+  cache[lamb1][dev] = n;
+  known[lamb1][dev] = true;
+  return n;
+}
+
+// Largest wavefront of either pass (voxels of one label).
+long long geo_max_wave(int Z, int Y, int X) {
+  long long m = 0;
+  for (int fwd = 1; fwd >= 0; --fwd) {
+    int t0, t1, step;
+    geo_t_range(Z, Y, X, fwd, &t0, &t1, &step);
+    for (int t = t0; step > 0 ? t <= t1 : t >= t1; t += step) {
+      const GeoWave w = geo_wave(Z, Y, X, fwd, t);
+      const long long n = (long long)w.nz * w.jmax;
+      m = n > m ? n : m;
+    }
+  }
+  return m;
+}
+
+// Scan mode of one call: cluster (true) or one launch per wavefront.
+// Auto takes the cluster scan while a wavefront needs at most 4 rounds of the
+// cluster's threads and a cluster fits on the device.
+int geo_resolve_mode(int Z, int Y, int X, bool lamb1, int mode, bool* cluster) {
+  const long long max_wave = geo_max_wave(Z, Y, X);
+  if (max_wave >= 0x7fffffffLL) return set_error(SI_ERR_LIMIT, "si_geo_scan: wavefront too large");
+  const int capacity = (mode == 1) ? 0 : geo_cluster_capacity(lamb1);
+  if (mode == 2 && capacity < 1)
+    return set_error(SI_ERR_CUDA, "si_geo_scan: a cluster of %d CTAs x %d threads cannot be launched here",
+                     kGeoCluster, kGeoClusterThreads);
+  *cluster = mode == 2 || (mode == 0 && capacity >= 1 && max_wave <= 4LL * kGeoCluster * kGeoClusterThreads);
+  return SI_OK;
+}
+
+}  // namespace
+}  // namespace si
+
+extern "C" int si_geo_scan_launches(int Z, int Y, int X, double lamb, int iterations, int mode,
+                                    long long* launches) {
+  clear_error();
+  if (!launches || Z < 1 || Y < 1 || X < 1 || iterations < 0 || mode < 0 || mode > 2)
+    return set_error(SI_ERR_ARG, "si_geo_scan_launches: bad arguments");
+  *launches = 0;
+  if (!geo_has_interior(Z, Y, X) || iterations == 0) return SI_OK;
+  bool cluster = false;
+  const int rc = geo_resolve_mode(Z, Y, X, lamb == 1.0, mode, &cluster);
+  if (rc) return rc;
+  if (cluster) {
+    *launches = 1;
+    return SI_OK;
+  }
+  long long n = 0;
+  for (int fwd = 1; fwd >= 0; --fwd) {
+    int t0, t1, step;
+    geo_t_range(Z, Y, X, fwd, &t0, &t1, &step);
+    for (int t = t0; step > 0 ? t <= t1 : t >= t1; t += step) n += geo_wave(Z, Y, X, fwd, t).nz > 0;
+  }
+  *launches = n * iterations;
+  return SI_OK;
+}
+
 extern "C" int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int nol, double lamb, int iterations,
-                           void* stream) {
+                           int mode, void* stream) {
   clear_error();
   if (!c || !img) return set_error(SI_ERR_ARG, "si_geo_scan: null pointer");
-  if (Z < 1 || Y < 1 || X < 1 || nol < 1 || iterations < 0) return set_error(SI_ERR_ARG, "si_geo_scan: bad arguments");
+  if (Z < 1 || Y < 1 || X < 1 || nol < 1 || iterations < 0 || mode < 0 || mode > 2)
+    return set_error(SI_ERR_ARG, "si_geo_scan: bad arguments");
   if ((long long)X + 2LL * Y + 4LL * Z > 0x7fffffffLL) return set_error(SI_ERR_LIMIT, "si_geo_scan: volume too large");
   if (!geo_has_interior(Z, Y, X) || iterations == 0) return SI_OK;
   GeoScanArgs a{};
@@ -335,6 +472,29 @@ extern "C" int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int 
   }
   const bool lamb1 = (lamb == 1.0);
   cudaStream_t st = as_stream(stream);
+  bool cluster = false;
+  const int rc_mode = geo_resolve_mode(Z, Y, X, lamb1, mode, &cluster);
+  if (rc_mode) return rc_mode;
+  if (cluster) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(kGeoCluster * nol));
+    cfg.blockDim = dim3(kGeoClusterThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kGeoCluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = lamb1 ? cudaLaunchKernelEx(&cfg, geo_cluster_scan_kernel<true>, a, iterations)
+                                : cudaLaunchKernelEx(&cfg, geo_cluster_scan_kernel<false>, a, iterations);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return set_error(SI_ERR_CUDA, "si_geo_scan: cluster launch failed: %s", cudaGetErrorString(e));
+    }
+    return check_launch("si_geo_scan");
+  }
   const int block = 256;
   for (int it = 0; it < iterations; ++it) {
     for (int fwd = 1; fwd >= 0; --fwd) {

@@ -54,9 +54,15 @@ def _device(device):
     return torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
 
 
-def scan_device(c: torch.Tensor, img: torch.Tensor, lamb: float = 1.0, iterations: int = 4) -> torch.Tensor:
+SCAN_AUTO, SCAN_WAVEFRONTS, SCAN_CLUSTER = 0, 1, 2
+
+
+def scan_device(c: torch.Tensor, img: torch.Tensor, lamb: float = 1.0, iterations: int = 4,
+                mode: int = SCAN_AUTO) -> torch.Tensor:
     """geodesic_raster_scan on device tensors: c float32 (nol, Z, Y, X) or
-    (Z, Y, X), updated in place; img float32 (Z, Y, X)."""
+    (Z, Y, X), updated in place; img float32 (Z, Y, X). mode: SCAN_WAVEFRONTS
+    (one launch per wavefront), SCAN_CLUSTER (one launch, a thread-block
+    cluster per map) or SCAN_AUTO; all give identical results."""
     if c.dtype != torch.float32 or img.dtype != torch.float32 or not (c.is_cuda and img.is_cuda):
         raise TypeError("scan_device: float32 CUDA tensors expected")
     if img.dim() != 3 or tuple(c.shape[-3:]) != tuple(img.shape) or c.dim() not in (3, 4):
@@ -66,8 +72,19 @@ def scan_device(c: torch.Tensor, img: torch.Tensor, lamb: float = 1.0, iteration
     Z, Y, X = img.shape
     nol = 1 if c.dim() == 3 else c.shape[0]
     if nol:
-        nat.call("si_geo_scan", _ptr(c), _ptr(img), Z, Y, X, nol, float(lamb), int(iterations), _stream())
+        nat.call("si_geo_scan", _ptr(c), _ptr(img), Z, Y, X, nol, float(lamb), int(iterations), int(mode),
+                 _stream())
     return c
+
+
+def scan_launches(shape, lamb: float = 1.0, iterations: int = 4, mode: int = SCAN_AUTO) -> int:
+    """Kernel launches one scan of this shape makes (1 in cluster mode), with
+    the automatic mode resolved on the current device."""
+    import ctypes
+
+    n = ctypes.c_longlong(0)
+    nat.call("si_geo_scan_launches", *map(int, shape), float(lamb), int(iterations), int(mode), ctypes.byref(n))
+    return int(n.value)
 
 
 def geodesic_raster_scan(img, c, lamb=1.0, iterations=4):

@@ -357,10 +357,19 @@ int si_geo_masks(const void* labels, int dtype, uint64_t n,
  * volumes c[nol][Z][Y][X] (float32, updated in place) over one float32 image
  * img[Z][Y][X]: `iterations` times a forward and a backward raster pass with
  * cost c[q] + (1 - lamb)|q - p| + lamb (img[p] - img[q])^2, results identical
- * to the sequential scan. One kernel launch per wavefront x + 2y + 4z (about
- * X + 2Y + 4Z per pass), all volumes in each launch. */
+ * to the sequential scan. The passes run as wavefronts x + 2y + 4z (about
+ * X + 2Y + 4Z per pass). mode 1: one kernel launch per wavefront, all volumes
+ * in each launch; mode 2: one launch in which a cluster of 8 CTAs per volume
+ * runs every wavefront, separated by the cluster barrier; mode 0 (auto): mode
+ * 2 while a wavefront holds at most 32768 voxels, else mode 1. */
 int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int nol,
-                double lamb, int iterations, void* stream);
+                double lamb, int iterations, int mode, void* stream);
+
+/* Host only: *launches = the kernel launches one si_geo_scan call with these
+ * arguments makes (1 in cluster mode, else one per non-empty wavefront and
+ * iteration), after resolving mode 0 on the current device. */
+int si_geo_scan_launches(int Z, int Y, int X, double lamb, int iterations,
+                         int mode, long long* launches);
 
 /* out[v] = slot_label[k] of the first slot k >= 1 whose distance is strictly
  * below the running minimum that starts at slot 0's, else 0 (the label loop of

@@ -107,17 +107,39 @@ def test_scan_against_oracle(lamb, iterations, cuda):
     want = G.raster_scan(img, c.copy(), lamb, iterations)
     got = D.geodesic_raster_scan(img, c.copy(), lamb, iterations)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    d_img = torch.from_numpy(img).to(cuda)
+    for mode in (D.SCAN_WAVEFRONTS, D.SCAN_CLUSTER):
+        d_c = torch.from_numpy(c).to(cuda)
+        D.scan_device(d_c, d_img, lamb, iterations, mode)
+        assert np.array_equal(d_c.cpu().numpy().view(np.uint32), want.view(np.uint32)), mode
 
 
-def test_all_labels_in_one_scan_equal_separate_scans(cuda):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_all_labels_in_one_scan_equal_separate_scans(mode, cuda):
     """si_geo_scan over nol stacked maps equals nol single-map scans."""
     rng = np.random.default_rng(4)
     img = torch.from_numpy(rng.random((17, 21, 25)).astype(np.float32)).to(cuda)
     c = torch.from_numpy(np.where(rng.random((4, 17, 21, 25)) < 0.02, 0.0, np.inf).astype(np.float32)).to(cuda)
-    sep = [D.scan_device(c[k].clone(), img) for k in range(4)]
-    D.scan_device(c, img)
+    sep = [D.scan_device(c[k].clone(), img, mode=mode) for k in range(4)]
+    D.scan_device(c, img, mode=mode)
     for k in range(4):
         assert torch.equal(c[k], sep[k]), k
+
+
+@pytest.mark.parametrize("shape,nol", [((40, 300, 500), 1), ((60, 200, 300), 2)])
+def test_cluster_scan_with_wide_wavefronts(shape, nol, cuda):
+    """Wavefronts of up to 9606 (40x300x500) and 8196 (60x200x300) voxels,
+    wider than one round of the cluster's 8192 threads, and the wavefront mode
+    on the same maps."""
+    rng = np.random.default_rng(shape[0])
+    img = rng.random(shape).astype(np.float32)
+    c = np.where(rng.random((nol,) + shape) < 0.001, 0.0, np.inf).astype(np.float32)
+    want = np.stack([G.raster_scan(img, c[k].copy(), 1.0, 1) for k in range(nol)])
+    d_img = torch.from_numpy(img).to(cuda)
+    for mode in (D.SCAN_WAVEFRONTS, D.SCAN_CLUSTER):
+        d_c = torch.from_numpy(c).to(cuda)
+        D.scan_device(d_c, d_img, 1.0, 1, mode)
+        assert np.array_equal(d_c.cpu().numpy().view(np.uint32), want.view(np.uint32)), mode
 
 
 def test_segment_plain_volume_against_oracle(cuda):
@@ -131,10 +153,11 @@ def test_segment_plain_volume_against_oracle(cuda):
 
 def test_entry_points_reject_bad_arguments(cuda):
     L = nat.lib()
-    assert L.si_geo_scan(None, None, 4, 4, 4, 1, 1.0, 1, None) == 1
+    x = torch.zeros(8, dtype=torch.float32, device=cuda)
+    assert L.si_geo_scan(None, None, 4, 4, 4, 1, 1.0, 1, 0, None) == 1
+    assert L.si_geo_scan(x.data_ptr(), x.data_ptr(), 2, 2, 2, 1, 1.0, 1, 3, None) == 1  # no mode 3
     assert L.si_geo_select(None, 1, 8, None, None, None) == 1
     assert L.si_geo_masks(None, 0, 8, None, 1, None, None) == 1
-    x = torch.zeros(8, dtype=torch.float32, device=cuda)
     mm = torch.zeros(4, dtype=torch.int32, device=cuda)
     assert L.si_geo_normalize(x.data_ptr(), 0, 0, x.data_ptr(), mm.data_ptr(), None) == 1
     assert L.si_geo_normalize(x.data_ptr(), 17, 8, x.data_ptr(), mm.data_ptr(), None) == 1
