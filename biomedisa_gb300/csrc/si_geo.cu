@@ -14,6 +14,8 @@
 // intensity difference and its square are binary32, the cost sum and the
 // comparison binary64, the store rounds to binary32.
 #include <cmath>
+#include <mutex>
+#include <vector>
 
 #include "si_common.cuh"
 #include "si_internal.h"
@@ -405,17 +407,124 @@ long long geo_max_wave(int Z, int Y, int X) {
   return m;
 }
 
-// Scan mode of one call: cluster (true) or one launch per wavefront.
-// Auto takes the cluster scan while a wavefront needs at most 4 rounds of the
-// cluster's threads and a cluster fits on the device.
+// Scan mode of one call: the cluster scan (mode 2) or wavefront launches.
 int geo_resolve_mode(int Z, int Y, int X, bool lamb1, int mode, bool* cluster) {
   const long long max_wave = geo_max_wave(Z, Y, X);
   if (max_wave >= 0x7fffffffLL) return set_error(SI_ERR_LIMIT, "si_geo_scan: wavefront too large");
-  const int capacity = (mode == 1) ? 0 : geo_cluster_capacity(lamb1);
-  if (mode == 2 && capacity < 1)
+  if (mode == 2 && geo_cluster_capacity(lamb1) < 1)
     return set_error(SI_ERR_CUDA, "si_geo_scan: a cluster of %d CTAs x %d threads cannot be launched here",
                      kGeoCluster, kGeoClusterThreads);
-  *cluster = mode == 2 || (mode == 0 && capacity >= 1 && max_wave <= 4LL * kGeoCluster * kGeoClusterThreads);
+  *cluster = (mode == 2);
+  return SI_OK;
+}
+
+// All wavefront launches of a scan, in order, on stream st.
+int geo_launch_waves(const GeoScanArgs& a, bool lamb1, int iterations, cudaStream_t st) {
+  const int block = 256;
+  for (int it = 0; it < iterations; ++it) {
+    for (int fwd = 1; fwd >= 0; --fwd) {
+      int t0, t1, step;
+      geo_t_range(a.Z, a.Y, a.X, fwd, &t0, &t1, &step);
+      for (int t = t0; step > 0 ? t <= t1 : t >= t1; t += step) {
+        const GeoWave w = geo_wave(a.Z, a.Y, a.X, fwd, t);
+        if (w.nz == 0) continue;
+        const long long threads = (long long)w.nz * w.jmax * a.nol;
+        const long long blocks = (threads + block - 1) / block;
+        if (blocks > 0x7fffffffLL) return set_error(SI_ERR_LIMIT, "si_geo_scan: wavefront too large");
+        if (lamb1)
+          geo_wave_kernel<true><<<(unsigned)blocks, block, 0, st>>>(a, w, fwd);
+        else
+          geo_wave_kernel<false><<<(unsigned)blocks, block, 0, st>>>(a, w, fwd);
+      }
+    }
+  }
+  return SI_OK;
+}
+
+// Instantiated CUDA graphs of whole scans (the wavefront launches of one
+// call, parameters included), keyed by every argument that enters them.
+// Mode 0 captures a scan the second time the same arguments come; mode 3 the
+// first time. At most kGeoGraphs graphs are kept (least recently used go).
+struct GeoGraphKey {
+  int dev;
+  const float* c;
+  const float* img;
+  int Z, Y, X, nol, iterations;
+  double lamb;
+  bool operator==(const GeoGraphKey& o) const {
+    return dev == o.dev && c == o.c && img == o.img && Z == o.Z && Y == o.Y && X == o.X && nol == o.nol &&
+           iterations == o.iterations && lamb == o.lamb;
+  }
+};
+
+struct GeoGraph {
+  GeoGraphKey key;
+  cudaGraphExec_t exec;
+  unsigned long long used;
+};
+
+constexpr size_t kGeoGraphs = 8;
+constexpr size_t kGeoSeen = 64;
+std::mutex g_geo_mu;
+std::vector<GeoGraph> g_geo_graphs;
+std::vector<GeoGraphKey> g_geo_seen;
+unsigned long long g_geo_clock = 0;
+cudaStream_t g_geo_capture[64];
+
+// Runs the scan through a cached graph; *done = false when the caller should
+// launch the wavefronts directly (mode 0, first call with these arguments).
+int geo_scan_graph(const GeoScanArgs& a, bool lamb1, int iterations, int mode, cudaStream_t st, bool* done) {
+  *done = false;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return SI_OK;
+  const GeoGraphKey key{dev, a.c, a.img, a.Z, a.Y, a.X, a.nol, iterations, a.lamb};
+  std::lock_guard<std::mutex> lock(g_geo_mu);
+  for (GeoGraph& g : g_geo_graphs)
+    if (g.key == key) {
+      g.used = ++g_geo_clock;
+      if (cudaGraphLaunch(g.exec, st) != cudaSuccess) return check_launch("si_geo_scan (graph launch)");
+      *done = true;
+      return SI_OK;
+    }
+  if (mode == 0) {
+    bool seen = false;
+    for (const GeoGraphKey& k : g_geo_seen) seen = seen || (k == key);
+    if (!seen) {
+      if (g_geo_seen.size() >= kGeoSeen) g_geo_seen.erase(g_geo_seen.begin());
+      g_geo_seen.push_back(key);
+      return SI_OK;
+    }
+  }
+  if (!g_geo_capture[dev] && cudaStreamCreateWithFlags(&g_geo_capture[dev], cudaStreamNonBlocking) != cudaSuccess)
+    return check_launch("si_geo_scan (capture stream)");
+  cudaStream_t cs = g_geo_capture[dev];
+  if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return check_launch("si_geo_scan (begin capture)");
+  const int rc = geo_launch_waves(a, lamb1, iterations, cs);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(cs, &graph);
+  if (rc || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    (void)cudaGetLastError();
+    return rc ? rc : set_error(SI_ERR_CUDA, "si_geo_scan: capture failed: %s", cudaGetErrorString(e));
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) {
+    (void)cudaGetLastError();
+    return set_error(SI_ERR_CUDA, "si_geo_scan: graph instantiation failed: %s", cudaGetErrorString(ei));
+  }
+  if (g_geo_graphs.size() >= kGeoGraphs) {
+    size_t old = 0;
+    for (size_t i = 1; i < g_geo_graphs.size(); ++i)
+      if (g_geo_graphs[i].used < g_geo_graphs[old].used) old = i;
+    cudaGraphExecDestroy(g_geo_graphs[old].exec);  // an in-flight graph is freed when it completes
+    g_geo_graphs.erase(g_geo_graphs.begin() + old);
+  }
+  g_geo_graphs.push_back(GeoGraph{key, exec, ++g_geo_clock});
+  if (cudaGraphLaunch(exec, st) != cudaSuccess) return check_launch("si_geo_scan (graph launch)");
+  *done = true;
   return SI_OK;
 }
 
@@ -425,7 +534,7 @@ int geo_resolve_mode(int Z, int Y, int X, bool lamb1, int mode, bool* cluster) {
 extern "C" int si_geo_scan_launches(int Z, int Y, int X, double lamb, int iterations, int mode,
                                     long long* launches) {
   clear_error();
-  if (!launches || Z < 1 || Y < 1 || X < 1 || iterations < 0 || mode < 0 || mode > 2)
+  if (!launches || Z < 1 || Y < 1 || X < 1 || iterations < 0 || mode < 0 || mode > 3)
     return set_error(SI_ERR_ARG, "si_geo_scan_launches: bad arguments");
   *launches = 0;
   if (!geo_has_interior(Z, Y, X) || iterations == 0) return SI_OK;
@@ -450,7 +559,7 @@ extern "C" int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int 
                            int mode, void* stream) {
   clear_error();
   if (!c || !img) return set_error(SI_ERR_ARG, "si_geo_scan: null pointer");
-  if (Z < 1 || Y < 1 || X < 1 || nol < 1 || iterations < 0 || mode < 0 || mode > 2)
+  if (Z < 1 || Y < 1 || X < 1 || nol < 1 || iterations < 0 || mode < 0 || mode > 3)
     return set_error(SI_ERR_ARG, "si_geo_scan: bad arguments");
   if ((long long)X + 2LL * Y + 4LL * Z > 0x7fffffffLL) return set_error(SI_ERR_LIMIT, "si_geo_scan: volume too large");
   if (!geo_has_interior(Z, Y, X) || iterations == 0) return SI_OK;
@@ -495,27 +604,13 @@ extern "C" int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int 
     }
     return check_launch("si_geo_scan");
   }
-  const int block = 256;
-  for (int it = 0; it < iterations; ++it) {
-    for (int fwd = 1; fwd >= 0; --fwd) {
-      int t0, t1, step;
-      geo_t_range(Z, Y, X, fwd, &t0, &t1, &step);
-      for (int t = t0; step > 0 ? t <= t1 : t >= t1; t += step) {
-        const GeoWave w = geo_wave(Z, Y, X, fwd, t);
-        if (w.nz == 0) continue;
-        const long long threads = (long long)w.nz * w.jmax * nol;
-        const long long blocks = (threads + block - 1) / block;
-        if (blocks > 0x7fffffffLL) return set_error(SI_ERR_LIMIT, "si_geo_scan: wavefront too large");
-        if (lamb1)
-          geo_wave_kernel<true><<<(unsigned)blocks, block, 0, st>>>(a, w, fwd);
-        else
-          geo_wave_kernel<false><<<(unsigned)blocks, block, 0, st>>>(a, w, fwd);
-      }
-    }
-    const int rc = check_launch("si_geo_scan");
-    if (rc) return rc;
+  if (mode == 0 || mode == 3) {
+    bool done = false;
+    const int rc = geo_scan_graph(a, lamb1, iterations, mode, st, &done);
+    if (rc || done) return rc;
   }
-  return SI_OK;
+  const int rc = geo_launch_waves(a, lamb1, iterations, st);
+  return rc ? rc : check_launch("si_geo_scan");
 }
 
 extern "C" int si_geo_select(const float* c, int nol, uint64_t n, const uint8_t* slot_label, uint8_t* out,

@@ -54,15 +54,17 @@ def _device(device):
     return torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
 
 
-SCAN_AUTO, SCAN_WAVEFRONTS, SCAN_CLUSTER = 0, 1, 2
+SCAN_AUTO, SCAN_WAVEFRONTS, SCAN_CLUSTER, SCAN_GRAPH = 0, 1, 2, 3
 
 
 def scan_device(c: torch.Tensor, img: torch.Tensor, lamb: float = 1.0, iterations: int = 4,
                 mode: int = SCAN_AUTO) -> torch.Tensor:
     """geodesic_raster_scan on device tensors: c float32 (nol, Z, Y, X) or
     (Z, Y, X), updated in place; img float32 (Z, Y, X). mode: SCAN_WAVEFRONTS
-    (one launch per wavefront), SCAN_CLUSTER (one launch, a thread-block
-    cluster per map) or SCAN_AUTO; all give identical results."""
+    (one launch per wavefront), SCAN_GRAPH (those launches replayed from a
+    cached CUDA graph), SCAN_CLUSTER (one launch, a thread-block cluster per
+    map) or SCAN_AUTO (direct launches on the first call with a set of
+    arguments, the graph from the second on); all give identical results."""
     if c.dtype != torch.float32 or img.dtype != torch.float32 or not (c.is_cuda and img.is_cuda):
         raise TypeError("scan_device: float32 CUDA tensors expected")
     if img.dim() != 3 or tuple(c.shape[-3:]) != tuple(img.shape) or c.dim() not in (3, 4):

@@ -358,10 +358,17 @@ int si_geo_masks(const void* labels, int dtype, uint64_t n,
  * img[Z][Y][X]: `iterations` times a forward and a backward raster pass with
  * cost c[q] + (1 - lamb)|q - p| + lamb (img[p] - img[q])^2, results identical
  * to the sequential scan. The passes run as wavefronts x + 2y + 4z (about
- * X + 2Y + 4Z per pass). mode 1: one kernel launch per wavefront, all volumes
- * in each launch; mode 2: one launch in which a cluster of 8 CTAs per volume
- * runs every wavefront, separated by the cluster barrier; mode 0 (auto): mode
- * 2 while a wavefront holds at most 32768 voxels, else mode 1. */
+ * X + 2Y + 4Z per pass).
+ *   mode 1: one kernel launch per wavefront, all volumes in each launch;
+ *   mode 3: the same launches captured once into a CUDA graph, which later
+ *           calls with the same arguments (pointers included) replay;
+ *   mode 0: mode 1 on the first call with a set of arguments, mode 3 from the
+ *           second on (the default);
+ *   mode 2: one launch in which a cluster of 8 CTAs per volume runs every
+ *           wavefront, separated by the cluster barrier.
+ * Modes 0 and 3 keep up to 8 instantiated graphs per process (graph
+ * instantiation allocates device memory; the least recently used graph is
+ * destroyed when a ninth is made). */
 int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int nol,
                 double lamb, int iterations, int mode, void* stream);
 

@@ -108,13 +108,36 @@ def test_scan_against_oracle(lamb, iterations, cuda):
     got = D.geodesic_raster_scan(img, c.copy(), lamb, iterations)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     d_img = torch.from_numpy(img).to(cuda)
-    for mode in (D.SCAN_WAVEFRONTS, D.SCAN_CLUSTER):
+    for mode in (D.SCAN_WAVEFRONTS, D.SCAN_CLUSTER, D.SCAN_GRAPH):
         d_c = torch.from_numpy(c).to(cuda)
         D.scan_device(d_c, d_img, lamb, iterations, mode)
         assert np.array_equal(d_c.cpu().numpy().view(np.uint32), want.view(np.uint32)), mode
 
 
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [0, 3])
+def test_scan_graph_replays(mode, cuda):
+    """Repeated scans of the same buffers: auto mode launches directly, then
+    captures, then replays its graph; graph mode captures on the first call.
+    Every call must give the oracle's maps."""
+    rng = np.random.default_rng(30 + mode)
+    img = rng.random((21, 18, 24)).astype(np.float32)
+    c0 = np.where(rng.random((2,) + img.shape) < 0.02, 0.0, np.inf).astype(np.float32)
+    want = np.stack([G.raster_scan(img, c0[k].copy(), 1.0, 4) for k in range(2)])
+    d_img = torch.from_numpy(img).to(cuda)
+    d_c0 = torch.from_numpy(c0).to(cuda)
+    buf = torch.empty_like(d_c0)
+    for call in range(4):
+        buf.copy_(d_c0)
+        D.scan_device(buf, d_img, 1.0, 4, mode)
+        assert np.array_equal(buf.cpu().numpy().view(np.uint32), want.view(np.uint32)), (mode, call)
+    other = torch.from_numpy(rng.random(img.shape).astype(np.float32)).to(cuda)  # same shape, other image
+    buf.copy_(d_c0)
+    D.scan_device(buf, other, 1.0, 4, mode)
+    want2 = np.stack([G.raster_scan(other.cpu().numpy(), c0[k].copy(), 1.0, 4) for k in range(2)])
+    assert np.array_equal(buf.cpu().numpy().view(np.uint32), want2.view(np.uint32))
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3])
 def test_all_labels_in_one_scan_equal_separate_scans(mode, cuda):
     """si_geo_scan over nol stacked maps equals nol single-map scans."""
     rng = np.random.default_rng(4)
@@ -155,7 +178,7 @@ def test_entry_points_reject_bad_arguments(cuda):
     L = nat.lib()
     x = torch.zeros(8, dtype=torch.float32, device=cuda)
     assert L.si_geo_scan(None, None, 4, 4, 4, 1, 1.0, 1, 0, None) == 1
-    assert L.si_geo_scan(x.data_ptr(), x.data_ptr(), 2, 2, 2, 1, 1.0, 1, 3, None) == 1  # no mode 3
+    assert L.si_geo_scan(x.data_ptr(), x.data_ptr(), 2, 2, 2, 1, 1.0, 1, 4, None) == 1  # no mode 4
     assert L.si_geo_select(None, 1, 8, None, None, None) == 1
     assert L.si_geo_masks(None, 0, 8, None, 1, None, None) == 1
     mm = torch.zeros(4, dtype=torch.int32, device=cuda)
