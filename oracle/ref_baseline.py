@@ -21,6 +21,8 @@ import numpy as np
 
 from ref_run import ref_lib
 
+import oracle
+
 
 def _threads() -> int:
     try:
@@ -85,6 +87,59 @@ def bounded_sample(work_img, work_labels, all_labels, z_slice, nbrw, sorw, targe
         "cores": _threads(),
         "seconds": dt,
         "steps": steps,
+        "kind": "reference",
         "sample": f"reference OpenCL walker (C, OpenMP) on the {seeds} seeds of rows {r0}-{r1} of crop z-slice "
                   f"{z_slice}, all {len(all_labels)} labels, nbrw={nbrw}, sorw={sorw}",
+    }
+
+
+def port_walk_sample(work_img, work_labels, all_labels, nbrw, sorw, z_slice, rows, nthreads=0):
+    """The oracle's C walker switched to the reference OpenCL kernel's
+    semantics (its RNG seeded by the global voxel index, expf weights, the
+    extended variance window; pinned bit for bit to the reference kernel by
+    tests/test_oracle_pin.py) over the seeds of rows [rows[0], rows[1]) of crop
+    slice z_slice. Returns (steps, seconds, seeds)."""
+    r0, r1 = rows
+    lab = np.full(work_labels.shape, -1, work_labels.dtype)
+    zs = slice(max(z_slice - 1, 0), z_slice + 2)
+    ys = slice(max(r0 - 1, 0), r1 + 1)
+    lab[zs, ys] = work_labels[zs, ys]
+    seeds = oracle.extract_seeds(work_img, lab, [(0, z_slice)], all_labels, var_mode="opencl")
+    Y, X = work_img.shape[1:]
+    row = (seeds.pos.astype(np.int64) // X) % Y
+    keep = (row >= r0) & (row < r1)
+    seeds = oracle.Seeds(**{k: getattr(seeds, k)[keep] for k in
+                            ("pos", "slot", "axis", "label", "b", "var", "rng_cuda", "rng_ocl")})
+    t0 = time.perf_counter()
+    oracle.walk_c(work_img, seeds, nbrw, sorw, 0, len(all_labels), rng="ref_mrg", weight="ref_expf",
+                  rng_index=seeds.rng_ocl, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return len(seeds) * nbrw * sorw, dt, len(seeds)
+
+
+def bounded_sample_port(work_img, work_labels, all_labels, z_slice, nbrw, sorw, target_seconds=12.0):
+    """bounded_sample with the oracle's restatement of the reference kernel,
+    for hosts where oracle/_ref cannot be built (no reference tree and no
+    extracted sources)."""
+    Y = work_img.shape[1]
+    mid = Y // 2
+    rows = 4
+    cores = _threads()
+    steps, dt, seeds = port_walk_sample(work_img, work_labels, all_labels, nbrw, sorw, z_slice, (mid, mid + rows),
+                                        cores)
+    rate = steps / max(dt, 1e-6)
+    per_row = max(steps / rows, 1.0)
+    want = int(min(max(target_seconds * rate / per_row, 1), Y - 2))
+    r0 = max(1, mid - want // 2)
+    r1 = min(Y - 1, r0 + want)
+    steps, dt, seeds = port_walk_sample(work_img, work_labels, all_labels, nbrw, sorw, z_slice, (r0, r1), cores)
+    return {
+        "value": steps / dt,
+        "unit": "walker-steps/s",
+        "cores": cores,
+        "seconds": dt,
+        "steps": steps,
+        "kind": "port",
+        "sample": f"the oracle's C restatement of the reference OpenCL walker (OpenMP) on the {seeds} seeds of rows "
+                  f"{r0}-{r1} of crop z-slice {z_slice}, all {len(all_labels)} labels, nbrw={nbrw}, sorw={sorw}",
     }

@@ -217,3 +217,26 @@ def test_large_seeding_matches_reference_large_kernel_live():
                                   a.ctypes.data_as(ctypes.c_void_p), X, Y, Z, ind.ctypes.data_as(ctypes.c_void_p),
                                   40, 2)
         assert np.array_equal(a, hits[s].astype(np.float32)), f"label {seg}"
+
+
+def test_cpu_baseline_port_walks_the_reference_sample():
+    """The reference arm's fallback (the oracle's restatement of the reference
+    OpenCL walker, for hosts without oracle/_ref) walks the same seeds of a
+    band of rows as the reference kernel's own sample."""
+    import ref_baseline
+    from biomedisa_gb300 import synthetic as S
+
+    img, lab, _ = S.plain_volume(seed=2, shape=(24, 30, 28), z_every=6, semi=(4, 9))
+    labelData, all_labels = O.pre_processing(lab)
+    data = np.pad(O.normalize_image(img), 1)
+    labc = np.pad(labelData, 1)
+    z = O.read_labeled_slices(labc)[0][1]
+    port = ref_baseline.port_walk_sample(data, labc, all_labels, 2, 20, z, (8, 14), 1)
+    assert port[2] > 0 and port[0] == port[2] * 2 * 20
+    out = ref_baseline.bounded_sample_port(data, labc, all_labels, z, 2, 20, 0.05)
+    assert out["kind"] == "port" and out["value"] > 0
+    try:
+        ref = ref_baseline.ocl_walk_sample(data, labc, all_labels, 2, 20, z, (8, 14))
+    except FileNotFoundError:
+        pytest.skip("oracle/_ref not built here")
+    assert ref[2] == port[2]
