@@ -893,7 +893,7 @@ def run_geodesic_bench(args, wl):
             torch.cuda.synchronize()
             t_job.append(ev[0].elapsed_time(ev[1]))
         cbuf = torch.empty_like(c0)  # one buffer: auto mode keys its graph by the pointers
-        for mode in (D.SCAN_AUTO, D.SCAN_WAVEFRONTS, D.SCAN_CLUSTER):
+        for mode in range(6):
             for _ in range(2):  # untimed: auto mode captures its graph on the second call
                 cbuf.copy_(c0)
                 D.scan_device(cbuf, work, mode=mode)
@@ -938,17 +938,19 @@ def run_geodesic_bench(args, wl):
         "e2e": {"value": n_vox / e2e_s, "unit": "voxels/s", "seconds": e2e_s,
                 "h2d_bytes_per_step": int(img.nbytes + lab.nbytes), "d2h_bytes_per_step": int(r.nbytes)},
         "gpu_launches": 3 + 1 + 1 + scan_launches + 1,
-        "scan_ms": scan_ms, "scan_mode": "wavefront launches replayed from a cached CUDA graph",
-        "scan_ms_direct_launches": scan_ms_mode[D.SCAN_WAVEFRONTS],
-        "scan_ms_cluster": scan_ms_mode[D.SCAN_CLUSTER],
-        "wavefronts_per_scan": waves, "us_per_wavefront": scan_ms * 1e3 / waves,
+        "scan_ms": scan_ms, "scan_mode": "tiles in skewed coordinates, launches replayed from a cached CUDA graph",
+        "scan_ms_by_mode": {"tiles": scan_ms_mode[D.SCAN_TILES], "tiles_graph": scan_ms_mode[D.SCAN_TILE_GRAPH],
+                            "wavefronts": scan_ms_mode[D.SCAN_WAVEFRONTS],
+                            "wavefronts_graph": scan_ms_mode[D.SCAN_WAVEFRONT_GRAPH],
+                            "cluster": scan_ms_mode[D.SCAN_CLUSTER]},
+        "wavefronts_per_scan": waves, "launches_per_scan": scan_launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": None,
-                     "note": f"the scan kernel over one scan ({scan_launches} launch(es), {waves} wavefronts, "
+                     "note": f"geo_tile_kernel over one scan ({scan_launches} launches of tile-wavefronts, "
                              f"{nol} labels): algorithmic bytes = 8 B per voxel-label update (read + write the "
                              "distance) + 4 B per voxel update (image) / CUDA-event scan duration; latency-bound: "
-                             "the wavefronts x + 2y + 4z run one after another; peak "
-                             f"{'measured' if pk else 'fallback'} HBM"},
+                             "the tile-wavefronts run one after another, each tile steps through its 32 planes; "
+                             f"peak {'measured' if pk else 'fallback'} HBM"},
         "clocks": clocks.summary(),
     }
     if not args.no_cpu_baseline:

@@ -81,6 +81,7 @@ _SIGNATURES = {
     "si_geo_masks": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_int, _c_void_p, _c_void_p],
     "si_geo_scan": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, ctypes.c_double, _c_int, _c_int,
                     _c_void_p],
+    "si_geo_tile_visit_order": [_c_int, _c_int, _c_int, _c_int, _c_void_p, _c_void_p, _c_void_p],
     "si_geo_scan_launches": [_c_int, _c_int, _c_int, ctypes.c_double, _c_int, _c_int, _c_void_p],
     "si_geo_select": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_void_p, _c_void_p],
     "si_geo_visit_order": [_c_int, _c_int, _c_int, _c_int, _c_void_p],

@@ -89,6 +89,7 @@ struct GeoScanArgs {
   int Z, Y, X, nol;
   long long V;
   long long off[13];  // forward linear offsets
+  int box_off[13];    // the same offsets in the tiled kernel's shared-memory box
   double w[13];       // (1 - lamb) * |offset|
   double lamb;
 };
@@ -143,6 +144,141 @@ __global__ void __launch_bounds__(256) geo_wave_kernel(GeoScanArgs a, GeoWave w,
   int z, y, x;
   if (!geo_wave_voxel(a.Y, a.X, w, zi, j, &z, &y, &x)) return;
   geo_update<kLamb1, false>(a, a.c + (long long)k * a.V, ((long long)z * a.Y + y) * a.X + x, fwd);
+}
+
+// ---------------------------------------------------------------------------
+// Tiled mode. In the skewed coordinates p = s(x + 2y + 4z), q = s(y + 2z),
+// r = s z (s = +1 forward, -1 backward) every neighbour a voxel reads lies at
+// (p + dp, q + dq, r + dr) with dp in [-7, -1], dq in [-3, 0], dr in [-1, 0]
+// (the same 13 offsets for both passes). Rectangular tiles of kTileP x kTileQ
+// x kTileR in (p, q, r) are therefore legal: a voxel's neighbours lie in its
+// own tile or in tiles whose indices are all <= and one <, i.e. in an earlier
+// tile-wavefront S = ip + iq + ir. One launch per S; a CTA takes one tile of
+// one label, stages the tile and its halo (7 in p, 3 in q, 1 in r) of the
+// distance map and the image in shared memory, updates its voxels plane by
+// plane in p with a CTA barrier between planes (planes of equal p are
+// independent), and writes the tile back.
+// ---------------------------------------------------------------------------
+constexpr int kTileP = 32, kTileQ = 32, kTileR = 8;
+constexpr int kBoxP = kTileP + 7, kBoxQ = kTileQ + 3, kBoxR = kTileR + 1;
+constexpr int kBoxCells = kBoxP * kBoxQ * kBoxR;
+constexpr int kTileThreads = kTileQ * kTileR;
+constexpr size_t kTileSmem = 2 * sizeof(float) * kBoxCells;
+
+struct GeoTiling {
+  int s;             // +1 forward, -1 backward
+  int zlo, zhi;      // z range of the pass
+  int pb, qb, rb;    // smallest transformed coordinates over the pass's domain
+  int ntp, ntq, ntr;  // tiles along p, q, r
+};
+
+__host__ __device__ inline GeoTiling geo_tiling(int Z, int Y, int X, int fwd) {
+  GeoTiling g;
+  g.s = fwd ? 1 : -1;
+  g.zlo = fwd ? 1 : 0;
+  g.zhi = fwd ? Z - 1 : Z - 2;
+  const int pmin = 1 + 2 + 4 * g.zlo, pmax = (X - 2) + 2 * (Y - 2) + 4 * g.zhi;
+  const int qmin = 1 + 2 * g.zlo, qmax = (Y - 2) + 2 * g.zhi;
+  g.pb = fwd ? pmin : -pmax;
+  g.qb = fwd ? qmin : -qmax;
+  g.rb = fwd ? g.zlo : -g.zhi;
+  g.ntp = (pmax - pmin + kTileP) / kTileP;
+  g.ntq = (qmax - qmin + kTileQ) / kTileQ;
+  g.ntr = (g.zhi - g.zlo + kTileR) / kTileR;
+  return g;
+}
+
+// Volume coordinates of transformed (p, q, r).
+__host__ __device__ inline void geo_unskew(const GeoTiling& g, int p, int q, int r, int* z, int* y, int* x) {
+  *z = g.s * r;
+  *y = g.s * q - 2 * *z;
+  *x = g.s * p - 2 * *y - 4 * *z;
+}
+
+// Voxel at step k of column (cq, cr) of tile (ip, iq, ir); false when it is
+// outside the pass's domain.
+__host__ __device__ inline bool geo_tile_voxel(const GeoTiling& g, int Y, int X, int ip, int iq, int ir, int cq,
+                                               int cr, int k, int* z, int* y, int* x) {
+  geo_unskew(g, g.pb + ip * kTileP + k, g.qb + iq * kTileQ + cq, g.rb + ir * kTileR + cr, z, y, x);
+  return *z >= g.zlo && *z <= g.zhi && *y >= 1 && *y <= Y - 2 && *x >= 1 && *x <= X - 2;
+}
+
+// Shared-memory box cell of transformed offset (dp, dq, dr) from the tile's
+// corner cell (7, 3, 1).
+__host__ __device__ constexpr int geo_box_cell(int bp, int bq, int br) { return (br * kBoxQ + bq) * kBoxP + bp; }
+
+// Box offset of neighbour n: (dp, dq, dr) = (dx + 2dy + 4dz, dy + 2dz, dz).
+inline int geo_box_offset(int n) {
+  const int dz = kGeoOff[n][0], dy = kGeoOff[n][1], dx = kGeoOff[n][2];
+  return geo_box_cell(dx + 2 * dy + 4 * dz, dy + 2 * dz, dz);
+}
+
+template <bool kLamb1>
+__global__ void __launch_bounds__(kTileThreads) geo_tile_kernel(GeoScanArgs a, GeoTiling g, int S) {
+  extern __shared__ float smem[];
+  float* sc = smem;              // distances of the box
+  float* si = smem + kBoxCells;  // image of the box
+  const int iq = blockIdx.x % g.ntq, ir = blockIdx.x / g.ntq;
+  const int ip = S - iq - ir;
+  if (ip < 0 || ip >= g.ntp || ir >= g.ntr) return;  // uniform over the CTA
+  float* cl = a.c + (long long)blockIdx.y * a.V;
+  const int cq = threadIdx.x % kTileQ, cr = threadIdx.x / kTileQ;
+  bool any = false;
+  for (int k = 0; k < kTileP; ++k) {
+    int z, y, x;
+    any = any || geo_tile_voxel(g, a.Y, a.X, ip, iq, ir, cq, cr, k, &z, &y, &x);
+  }
+  if (!__syncthreads_or(any)) return;  // no voxel of the domain in this tile
+  const int p0 = g.pb + ip * kTileP - 7, q0 = g.qb + iq * kTileQ - 3, r0 = g.rb + ir * kTileR - 1;
+  for (int cell = threadIdx.x; cell < kBoxCells; cell += kTileThreads) {
+    const int bp = cell % kBoxP, bq = (cell / kBoxP) % kBoxQ, br = cell / (kBoxP * kBoxQ);
+    int z, y, x;
+    geo_unskew(g, p0 + bp, q0 + bq, r0 + br, &z, &y, &x);
+    if (z >= 0 && z < a.Z && y >= 0 && y < a.Y && x >= 0 && x < a.X) {
+      const long long v = ((long long)z * a.Y + y) * a.X + x;
+      sc[cell] = cl[v];
+      si[cell] = a.img[v];
+    } else {
+      sc[cell] = __uint_as_float(0x7f800000u);
+      si[cell] = 0.0f;
+    }
+  }
+  __syncthreads();
+  for (int k = 0; k < kTileP; ++k) {
+    int z, y, x;
+    if (geo_tile_voxel(g, a.Y, a.X, ip, iq, ir, cq, cr, k, &z, &y, &x)) {
+      const int own = geo_box_cell(k + 7, cq + 3, cr + 1);
+      const float iv = si[own];
+      if (kLamb1) {
+        float best = sc[own];
+#pragma unroll
+        for (int n = 0; n < 13; ++n) {
+          const int nb = own + a.box_off[n];
+          const float diff = __fsub_rn(iv, si[nb]);
+          const float cost = __fadd_rn(sc[nb], __fmul_rn(diff, diff));
+          if (cost < best) best = cost;
+        }
+        sc[own] = best;
+      } else {
+        double best = (double)sc[own];
+#pragma unroll
+        for (int n = 0; n < 13; ++n) {
+          const int nb = own + a.box_off[n];
+          const float diff = __fsub_rn(iv, si[nb]);
+          const double sq = (double)__fmul_rn(diff, diff);
+          const double cost = __dadd_rn(__dadd_rn((double)sc[nb], a.w[n]), __dmul_rn(a.lamb, sq));
+          if (cost < best) best = cost;
+        }
+        sc[own] = __double2float_rn(best);
+      }
+    }
+    __syncthreads();
+  }
+  for (int k = 0; k < kTileP; ++k) {
+    int z, y, x;
+    if (geo_tile_voxel(g, a.Y, a.X, ip, iq, ir, cq, cr, k, &z, &y, &x))
+      cl[((long long)z * a.Y + y) * a.X + x] = sc[geo_box_cell(k + 7, cq + 3, cr + 1)];
+  }
 }
 
 // Cluster mode: one thread-block cluster of kGeoCluster CTAs per label runs
@@ -418,8 +554,40 @@ int geo_resolve_mode(int Z, int Y, int X, bool lamb1, int mode, bool* cluster) {
   return SI_OK;
 }
 
-// All wavefront launches of a scan, in order, on stream st.
-int geo_launch_waves(const GeoScanArgs& a, bool lamb1, int iterations, cudaStream_t st) {
+// Opt-in shared memory of the tiled kernel (once per device, outside any capture).
+int geo_tile_prepare() {
+  static bool done[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return check_launch("si_geo_scan (device)");
+  if (done[dev]) return SI_OK;
+  if (cudaFuncSetAttribute(geo_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(geo_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem) !=
+          cudaSuccess)
+    return check_launch("si_geo_scan (tile shared memory)");
+  done[dev] = true;
+  return SI_OK;
+}
+
+// All launches of a scan, in order, on stream st: one per tile-wavefront
+// (tiled) or one per wavefront.
+int geo_launch_scan(const GeoScanArgs& a, bool lamb1, int iterations, bool tiled, cudaStream_t st) {
+  if (tiled) {
+    for (int it = 0; it < iterations; ++it)
+      for (int fwd = 1; fwd >= 0; --fwd) {
+        const GeoTiling g = geo_tiling(a.Z, a.Y, a.X, fwd);
+        const long long ncta = (long long)g.ntq * g.ntr;
+        if (ncta > 0x7fffffffLL) return set_error(SI_ERR_LIMIT, "si_geo_scan: too many tiles");
+        const dim3 grid((unsigned)ncta, (unsigned)a.nol);
+        for (int S = 0; S <= g.ntp + g.ntq + g.ntr - 3; ++S) {
+          if (lamb1)
+            geo_tile_kernel<true><<<grid, kTileThreads, kTileSmem, st>>>(a, g, S);
+          else
+            geo_tile_kernel<false><<<grid, kTileThreads, kTileSmem, st>>>(a, g, S);
+        }
+      }
+    return SI_OK;
+  }
   const int block = 256;
   for (int it = 0; it < iterations; ++it) {
     for (int fwd = 1; fwd >= 0; --fwd) {
@@ -449,11 +617,11 @@ struct GeoGraphKey {
   int dev;
   const float* c;
   const float* img;
-  int Z, Y, X, nol, iterations;
+  int Z, Y, X, nol, iterations, tiled;
   double lamb;
   bool operator==(const GeoGraphKey& o) const {
     return dev == o.dev && c == o.c && img == o.img && Z == o.Z && Y == o.Y && X == o.X && nol == o.nol &&
-           iterations == o.iterations && lamb == o.lamb;
+           iterations == o.iterations && tiled == o.tiled && lamb == o.lamb;
   }
 };
 
@@ -473,11 +641,12 @@ cudaStream_t g_geo_capture[64];
 
 // Runs the scan through a cached graph; *done = false when the caller should
 // launch the wavefronts directly (mode 0, first call with these arguments).
-int geo_scan_graph(const GeoScanArgs& a, bool lamb1, int iterations, int mode, cudaStream_t st, bool* done) {
+int geo_scan_graph(const GeoScanArgs& a, bool lamb1, int iterations, bool tiled, bool capture_first,
+                   cudaStream_t st, bool* done) {
   *done = false;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return SI_OK;
-  const GeoGraphKey key{dev, a.c, a.img, a.Z, a.Y, a.X, a.nol, iterations, a.lamb};
+  const GeoGraphKey key{dev, a.c, a.img, a.Z, a.Y, a.X, a.nol, iterations, tiled ? 1 : 0, a.lamb};
   std::lock_guard<std::mutex> lock(g_geo_mu);
   for (GeoGraph& g : g_geo_graphs)
     if (g.key == key) {
@@ -486,7 +655,7 @@ int geo_scan_graph(const GeoScanArgs& a, bool lamb1, int iterations, int mode, c
       *done = true;
       return SI_OK;
     }
-  if (mode == 0) {
+  if (!capture_first) {
     bool seen = false;
     for (const GeoGraphKey& k : g_geo_seen) seen = seen || (k == key);
     if (!seen) {
@@ -500,7 +669,7 @@ int geo_scan_graph(const GeoScanArgs& a, bool lamb1, int iterations, int mode, c
   cudaStream_t cs = g_geo_capture[dev];
   if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     return check_launch("si_geo_scan (begin capture)");
-  const int rc = geo_launch_waves(a, lamb1, iterations, cs);
+  const int rc = geo_launch_scan(a, lamb1, iterations, tiled, cs);
   cudaGraph_t graph = nullptr;
   const cudaError_t e = cudaStreamEndCapture(cs, &graph);
   if (rc || e != cudaSuccess) {
@@ -534,7 +703,7 @@ int geo_scan_graph(const GeoScanArgs& a, bool lamb1, int iterations, int mode, c
 extern "C" int si_geo_scan_launches(int Z, int Y, int X, double lamb, int iterations, int mode,
                                     long long* launches) {
   clear_error();
-  if (!launches || Z < 1 || Y < 1 || X < 1 || iterations < 0 || mode < 0 || mode > 3)
+  if (!launches || Z < 1 || Y < 1 || X < 1 || iterations < 0 || mode < 0 || mode > 5)
     return set_error(SI_ERR_ARG, "si_geo_scan_launches: bad arguments");
   *launches = 0;
   if (!geo_has_interior(Z, Y, X) || iterations == 0) return SI_OK;
@@ -547,6 +716,11 @@ extern "C" int si_geo_scan_launches(int Z, int Y, int X, double lamb, int iterat
   }
   long long n = 0;
   for (int fwd = 1; fwd >= 0; --fwd) {
+    if (mode == 0 || mode == 4 || mode == 5) {
+      const GeoTiling g = geo_tiling(Z, Y, X, fwd);
+      n += g.ntp + g.ntq + g.ntr - 2;
+      continue;
+    }
     int t0, t1, step;
     geo_t_range(Z, Y, X, fwd, &t0, &t1, &step);
     for (int t = t0; step > 0 ? t <= t1 : t >= t1; t += step) n += geo_wave(Z, Y, X, fwd, t).nz > 0;
@@ -559,7 +733,7 @@ extern "C" int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int 
                            int mode, void* stream) {
   clear_error();
   if (!c || !img) return set_error(SI_ERR_ARG, "si_geo_scan: null pointer");
-  if (Z < 1 || Y < 1 || X < 1 || nol < 1 || iterations < 0 || mode < 0 || mode > 3)
+  if (Z < 1 || Y < 1 || X < 1 || nol < 1 || iterations < 0 || mode < 0 || mode > 5)
     return set_error(SI_ERR_ARG, "si_geo_scan: bad arguments");
   if ((long long)X + 2LL * Y + 4LL * Z > 0x7fffffffLL) return set_error(SI_ERR_LIMIT, "si_geo_scan: volume too large");
   if (!geo_has_interior(Z, Y, X) || iterations == 0) return SI_OK;
@@ -575,6 +749,7 @@ extern "C" int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int 
   const long long YX = (long long)Y * X;
   for (int n = 0; n < 13; ++n) {
     a.off[n] = kGeoOff[n][0] * YX + (long long)kGeoOff[n][1] * X + kGeoOff[n][2];
+    a.box_off[n] = geo_box_offset(n);
     const int nzc = (kGeoOff[n][0] != 0) + (kGeoOff[n][1] != 0) + (kGeoOff[n][2] != 0);
     const double d = nzc == 3 ? std::sqrt(3.0) : nzc == 2 ? std::sqrt(2.0) : 1.0;
     a.w[n] = (1.0 - lamb) * d;
@@ -604,12 +779,17 @@ extern "C" int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int 
     }
     return check_launch("si_geo_scan");
   }
-  if (mode == 0 || mode == 3) {
+  const bool tiled = (mode == 0 || mode == 4 || mode == 5);
+  if (tiled) {
+    const int rc = geo_tile_prepare();
+    if (rc) return rc;
+  }
+  if (mode == 0 || mode == 3 || mode == 5) {
     bool done = false;
-    const int rc = geo_scan_graph(a, lamb1, iterations, mode, st, &done);
+    const int rc = geo_scan_graph(a, lamb1, iterations, tiled, mode != 0, st, &done);
     if (rc || done) return rc;
   }
-  const int rc = geo_launch_waves(a, lamb1, iterations, st);
+  const int rc = geo_launch_scan(a, lamb1, iterations, tiled, st);
   return rc ? rc : check_launch("si_geo_scan");
 }
 
@@ -646,5 +826,48 @@ extern "C" int si_geo_visit_order(int Z, int Y, int X, int fwd, int32_t* t_of_vo
         t_of_voxel[v] = t;
       }
   }
+  return SI_OK;
+}
+
+extern "C" int si_geo_tile_visit_order(int Z, int Y, int X, int fwd, int32_t* wave, int32_t* tile, int32_t* step) {
+  clear_error();
+  if (!wave || !tile || !step || Z < 1 || Y < 1 || X < 1)
+    return set_error(SI_ERR_ARG, "si_geo_tile_visit_order: bad arguments");
+  const long long V = (long long)Z * Y * X;
+  for (long long v = 0; v < V; ++v) wave[v] = tile[v] = step[v] = -1;
+  if (!geo_has_interior(Z, Y, X)) return SI_OK;
+  const GeoTiling g = geo_tiling(Z, Y, X, fwd ? 1 : 0);
+  for (int S = 0; S <= g.ntp + g.ntq + g.ntr - 3; ++S)
+    for (int ir = 0; ir < g.ntr; ++ir)
+      for (int iq = 0; iq < g.ntq; ++iq) {
+        const int ip = S - iq - ir;
+        if (ip < 0 || ip >= g.ntp) continue;
+        const int p0 = g.pb + ip * kTileP - 7, q0 = g.qb + iq * kTileQ - 3, r0 = g.rb + ir * kTileR - 1;
+        for (int cr = 0; cr < kTileR; ++cr)
+          for (int cq = 0; cq < kTileQ; ++cq)
+            for (int k = 0; k < kTileP; ++k) {
+              int z, y, x;
+              if (!geo_tile_voxel(g, Y, X, ip, iq, ir, cq, cr, k, &z, &y, &x)) continue;
+              const long long v = ((long long)z * Y + y) * X + x;
+              if (wave[v] != -1)
+                return set_error(SI_ERR_LIMIT, "si_geo_tile_visit_order: voxel (%d,%d,%d) visited twice", z, y, x);
+              wave[v] = S;
+              tile[v] = (ip * g.ntr + ir) * g.ntq + iq;
+              step[v] = k;
+              // every neighbour the kernel reads: inside the box, and the voxel the scan reads
+              const int own = geo_box_cell(k + 7, cq + 3, cr + 1);
+              for (int n = 0; n < 13; ++n) {
+                const int cell = own + geo_box_offset(n);
+                if (cell < 0 || cell >= kBoxCells)
+                  return set_error(SI_ERR_LIMIT, "si_geo_tile_visit_order: neighbour %d outside the box", n);
+                const int bp = cell % kBoxP, bq = (cell / kBoxP) % kBoxQ, br = cell / (kBoxP * kBoxQ);
+                int nz, ny, nx;
+                geo_unskew(g, p0 + bp, q0 + bq, r0 + br, &nz, &ny, &nx);
+                const int sg = fwd ? 1 : -1;
+                if (nz != z + sg * kGeoOff[n][0] || ny != y + sg * kGeoOff[n][1] || nx != x + sg * kGeoOff[n][2])
+                  return set_error(SI_ERR_LIMIT, "si_geo_tile_visit_order: box neighbour %d is not the scan's", n);
+              }
+            }
+      }
   return SI_OK;
 }

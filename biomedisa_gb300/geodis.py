@@ -54,17 +54,19 @@ def _device(device):
     return torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
 
 
-SCAN_AUTO, SCAN_WAVEFRONTS, SCAN_CLUSTER, SCAN_GRAPH = 0, 1, 2, 3
+SCAN_AUTO, SCAN_WAVEFRONTS, SCAN_CLUSTER, SCAN_WAVEFRONT_GRAPH, SCAN_TILES, SCAN_TILE_GRAPH = range(6)
 
 
 def scan_device(c: torch.Tensor, img: torch.Tensor, lamb: float = 1.0, iterations: int = 4,
                 mode: int = SCAN_AUTO) -> torch.Tensor:
     """geodesic_raster_scan on device tensors: c float32 (nol, Z, Y, X) or
-    (Z, Y, X), updated in place; img float32 (Z, Y, X). mode: SCAN_WAVEFRONTS
-    (one launch per wavefront), SCAN_GRAPH (those launches replayed from a
-    cached CUDA graph), SCAN_CLUSTER (one launch, a thread-block cluster per
-    map) or SCAN_AUTO (direct launches on the first call with a set of
-    arguments, the graph from the second on); all give identical results."""
+    (Z, Y, X), updated in place; img float32 (Z, Y, X). mode: SCAN_TILES (one
+    launch per wavefront of 32x32x8 tiles in skewed coordinates, each tile in
+    shared memory), SCAN_TILE_GRAPH (those launches replayed from a cached
+    CUDA graph), SCAN_AUTO (SCAN_TILES on the first call with a set of
+    arguments, the graph from the second on), SCAN_WAVEFRONTS (one launch per
+    voxel wavefront), SCAN_WAVEFRONT_GRAPH, SCAN_CLUSTER (one launch, a
+    thread-block cluster per map); all give identical results."""
     if c.dtype != torch.float32 or img.dtype != torch.float32 or not (c.is_cuda and img.is_cuda):
         raise TypeError("scan_device: float32 CUDA tensors expected")
     if img.dim() != 3 or tuple(c.shape[-3:]) != tuple(img.shape) or c.dim() not in (3, 4):

@@ -359,18 +359,32 @@ int si_geo_masks(const void* labels, int dtype, uint64_t n,
  * cost c[q] + (1 - lamb)|q - p| + lamb (img[p] - img[q])^2, results identical
  * to the sequential scan. The passes run as wavefronts x + 2y + 4z (about
  * X + 2Y + 4Z per pass).
- *   mode 1: one kernel launch per wavefront, all volumes in each launch;
- *   mode 3: the same launches captured once into a CUDA graph, which later
- *           calls with the same arguments (pointers included) replay;
- *   mode 0: mode 1 on the first call with a set of arguments, mode 3 from the
+ *   mode 4: tiled: the voxels in skewed coordinates p = x + 2y + 4z,
+ *           q = y + 2z, r = z cut into 32 x 32 x 8 tiles; one launch per
+ *           tile-wavefront (about (X + 2Y + 4Z)/32 + (Y + 2Z)/32 + Z/8 per
+ *           pass), a CTA per tile and volume working in shared memory;
+ *   mode 5: mode 4 captured once into a CUDA graph, which later calls with
+ *           the same arguments (pointers included) replay;
+ *   mode 0: mode 4 on the first call with a set of arguments, mode 5 from the
  *           second on (the default);
+ *   mode 1: one kernel launch per wavefront, all volumes in each launch;
+ *   mode 3: mode 1 captured into a CUDA graph as mode 5 does;
  *   mode 2: one launch in which a cluster of 8 CTAs per volume runs every
  *           wavefront, separated by the cluster barrier.
- * Modes 0 and 3 keep up to 8 instantiated graphs per process (graph
+ * Modes 0, 3 and 5 keep up to 8 instantiated graphs per process (graph
  * instantiation allocates device memory; the least recently used graph is
  * destroyed when a ninth is made). */
 int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int nol,
                 double lamb, int iterations, int mode, void* stream);
+
+/* Host only (no device work): the launch plan of si_geo_scan's tiled modes
+ * for the forward (fwd = 1) or backward (fwd = 0) pass: per voxel the
+ * tile-wavefront (launch) wave[v], a tile id tile[v] and the plane step[v] at
+ * which its CTA updates it, -1 for voxels the pass leaves alone. Fails if a
+ * voxel would be updated twice or a shared-memory neighbour is not the voxel
+ * the sequential scan reads. Exposed for checking the order. */
+int si_geo_tile_visit_order(int Z, int Y, int X, int fwd, int32_t* wave,
+                            int32_t* tile, int32_t* step);
 
 /* Host only: *launches = the kernel launches one si_geo_scan call with these
  * arguments makes (1 in cluster mode, else one per non-empty wavefront and

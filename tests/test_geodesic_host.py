@@ -109,6 +109,44 @@ def test_visit_order_reproduces_raster_dependencies(shape):
             assert np.all(tq < tp) if fwd else np.all(tq > tp), (shape, fwd, (dz, dy, dx))
 
 
+def _tile_order(shape, fwd):
+    from biomedisa_gb300 import _native as nat
+
+    arrs = [np.empty(shape, np.int32) for _ in range(3)]
+    rc = nat.lib().si_geo_tile_visit_order(*shape, int(fwd), *(a.ctypes.data_as(ctypes.c_void_p) for a in arrs))
+    assert rc == 0, nat.lib().si_last_error()
+    return arrs
+
+
+TILE_SHAPES = SHAPES + [(40, 70, 90), (9, 130, 45), (70, 20, 33), (12, 12, 300)]
+
+
+@pytest.mark.parametrize("shape", TILE_SHAPES)
+def test_tile_order_reproduces_raster_dependencies(shape):
+    """Tiled mode: every neighbour a voxel reads (when the pass updates it)
+    is finished in an earlier launch, or earlier in the same tile; the
+    library also checks that each shared-memory neighbour is the scan's."""
+    Z, Y, X = shape
+    for fwd in (1, 0):
+        wave, tile, step = _tile_order(shape, fwd)
+        dom = np.zeros(shape, bool)
+        if Z >= 2 and Y >= 3 and X >= 3:
+            zs = slice(1, Z) if fwd else slice(0, Z - 1)
+            dom[zs, 1:Y - 1, 1:X - 1] = True
+        assert np.array_equal(wave >= 0, dom), (shape, fwd)
+        zz, yy, xx = np.nonzero(dom)
+        sign = 1 if fwd else -1
+        for dz, dy, dx in FWD * sign:
+            qz, qy, qx = zz + dz, yy + dy, xx + dx
+            inside = dom[qz, qy, qx]
+            wq, wp = wave[qz, qy, qx][inside], wave[zz, yy, xx][inside]
+            same = (wq == wp)
+            assert np.all(wq <= wp), (shape, fwd, (dz, dy, dx))
+            tq, tp = tile[qz, qy, qx][inside][same], tile[zz, yy, xx][inside][same]
+            sq, sp = step[qz, qy, qx][inside][same], step[zz, yy, xx][inside][same]
+            assert np.all(tq == tp) and np.all(sq < sp), (shape, fwd, (dz, dy, dx))
+
+
 # --- kernel arithmetic emulated on the launch plan ---------------------------
 
 def _emulate_scan(img, c, lamb, iterations):

@@ -108,13 +108,13 @@ def test_scan_against_oracle(lamb, iterations, cuda):
     got = D.geodesic_raster_scan(img, c.copy(), lamb, iterations)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     d_img = torch.from_numpy(img).to(cuda)
-    for mode in (D.SCAN_WAVEFRONTS, D.SCAN_CLUSTER, D.SCAN_GRAPH):
+    for mode in range(6):
         d_c = torch.from_numpy(c).to(cuda)
         D.scan_device(d_c, d_img, lamb, iterations, mode)
         assert np.array_equal(d_c.cpu().numpy().view(np.uint32), want.view(np.uint32)), mode
 
 
-@pytest.mark.parametrize("mode", [0, 3])
+@pytest.mark.parametrize("mode", [0, 3, 5])
 def test_scan_graph_replays(mode, cuda):
     """Repeated scans of the same buffers: auto mode launches directly, then
     captures, then replays its graph; graph mode captures on the first call.
@@ -137,7 +137,7 @@ def test_scan_graph_replays(mode, cuda):
     assert np.array_equal(buf.cpu().numpy().view(np.uint32), want2.view(np.uint32))
 
 
-@pytest.mark.parametrize("mode", [1, 2, 3])
+@pytest.mark.parametrize("mode", [1, 2, 3, 4, 5])
 def test_all_labels_in_one_scan_equal_separate_scans(mode, cuda):
     """si_geo_scan over nol stacked maps equals nol single-map scans."""
     rng = np.random.default_rng(4)
@@ -159,10 +159,25 @@ def test_cluster_scan_with_wide_wavefronts(shape, nol, cuda):
     c = np.where(rng.random((nol,) + shape) < 0.001, 0.0, np.inf).astype(np.float32)
     want = np.stack([G.raster_scan(img, c[k].copy(), 1.0, 1) for k in range(nol)])
     d_img = torch.from_numpy(img).to(cuda)
-    for mode in (D.SCAN_WAVEFRONTS, D.SCAN_CLUSTER):
+    for mode in (D.SCAN_WAVEFRONTS, D.SCAN_CLUSTER, D.SCAN_TILES):
         d_c = torch.from_numpy(c).to(cuda)
         D.scan_device(d_c, d_img, 1.0, 1, mode)
         assert np.array_equal(d_c.cpu().numpy().view(np.uint32), want.view(np.uint32)), mode
+
+
+@pytest.mark.parametrize("shape", [(40, 70, 90), (9, 130, 45), (70, 20, 33), (12, 12, 300), (3, 3, 3), (2, 9, 40)])
+def test_tiled_scan_shapes(shape, cuda):
+    """The tiled scan on shapes with several tiles along every axis, thin
+    volumes and a single interior voxel, lamb 1 and 0.6."""
+    rng = np.random.default_rng(sum(shape))
+    img = rng.random(shape).astype(np.float32)
+    c = np.where(rng.random((2,) + shape) < 0.01, 0.0, np.inf).astype(np.float32)
+    d_img = torch.from_numpy(img).to(cuda)
+    for lamb, it in ((1.0, 2), (0.6, 1)):
+        want = np.stack([G.raster_scan(img, c[k].copy(), lamb, it) for k in range(2)])
+        d_c = torch.from_numpy(c).to(cuda)
+        D.scan_device(d_c, d_img, lamb, it, D.SCAN_TILES)
+        assert np.array_equal(d_c.cpu().numpy().view(np.uint32), want.view(np.uint32)), (shape, lamb)
 
 
 def test_segment_plain_volume_against_oracle(cuda):
@@ -178,7 +193,7 @@ def test_entry_points_reject_bad_arguments(cuda):
     L = nat.lib()
     x = torch.zeros(8, dtype=torch.float32, device=cuda)
     assert L.si_geo_scan(None, None, 4, 4, 4, 1, 1.0, 1, 0, None) == 1
-    assert L.si_geo_scan(x.data_ptr(), x.data_ptr(), 2, 2, 2, 1, 1.0, 1, 4, None) == 1  # no mode 4
+    assert L.si_geo_scan(x.data_ptr(), x.data_ptr(), 2, 2, 2, 1, 1.0, 1, 6, None) == 1  # no mode 6
     assert L.si_geo_select(None, 1, 8, None, None, None) == 1
     assert L.si_geo_masks(None, 0, 8, None, 1, None, None) == 1
     mm = torch.zeros(4, dtype=torch.int32, device=cuda)
