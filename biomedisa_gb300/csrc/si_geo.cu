@@ -164,6 +164,8 @@ constexpr int kBoxP = kTileP + 7, kBoxQ = kTileQ + 3, kBoxR = kTileR + 1;
 constexpr int kBoxCells = kBoxP * kBoxQ * kBoxR;
 constexpr int kTileThreads = kTileQ * kTileR;
 constexpr size_t kTileSmem = 2 * sizeof(float) * kBoxCells;
+constexpr int kStageBatch = 8;
+constexpr int kStageRounds = (kBoxCells + kTileThreads - 1) / kTileThreads;  // cells per thread, rounded up
 
 struct GeoTiling {
   int s;             // +1 forward, -1 backward
@@ -230,17 +232,33 @@ __global__ void __launch_bounds__(kTileThreads) geo_tile_kernel(GeoScanArgs a, G
   }
   if (!__syncthreads_or(any)) return;  // no voxel of the domain in this tile
   const int p0 = g.pb + ip * kTileP - 7, q0 = g.qb + iq * kTileQ - 3, r0 = g.rb + ir * kTileR - 1;
-  for (int cell = threadIdx.x; cell < kBoxCells; cell += kTileThreads) {
-    const int bp = cell % kBoxP, bq = (cell / kBoxP) % kBoxQ, br = cell / (kBoxP * kBoxQ);
-    int z, y, x;
-    geo_unskew(g, p0 + bp, q0 + bq, r0 + br, &z, &y, &x);
-    if (z >= 0 && z < a.Z && y >= 0 && y < a.Y && x >= 0 && x < a.X) {
-      const long long v = ((long long)z * a.Y + y) * a.X + x;
-      sc[cell] = cl[v];
-      si[cell] = a.img[v];
-    } else {
-      sc[cell] = __uint_as_float(0x7f800000u);
-      si[cell] = 0.0f;
+  // staging in batches of kStageBatch cells per thread: all loads of a batch
+  // are issued before the first shared-memory store waits for one
+  for (int b = 0; b < kStageRounds; b += kStageBatch) {
+    float vc[kStageBatch], vi[kStageBatch];
+#pragma unroll
+    for (int u = 0; u < kStageBatch; ++u) {
+      const int cell = threadIdx.x + (b + u) * kTileThreads;
+      vc[u] = __uint_as_float(0x7f800000u);
+      vi[u] = 0.0f;
+      if (cell < kBoxCells) {
+        const int bp = cell % kBoxP, bq = (cell / kBoxP) % kBoxQ, br = cell / (kBoxP * kBoxQ);
+        int z, y, x;
+        geo_unskew(g, p0 + bp, q0 + bq, r0 + br, &z, &y, &x);
+        if (z >= 0 && z < a.Z && y >= 0 && y < a.Y && x >= 0 && x < a.X) {
+          const long long v = ((long long)z * a.Y + y) * a.X + x;
+          vc[u] = cl[v];
+          vi[u] = a.img[v];
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kStageBatch; ++u) {
+      const int cell = threadIdx.x + (b + u) * kTileThreads;
+      if (cell < kBoxCells) {
+        sc[cell] = vc[u];
+        si[cell] = vi[u];
+      }
     }
   }
   __syncthreads();
