@@ -50,9 +50,10 @@ def test_oracle_scan_matches_reference_fixtures():
 def test_oracle_matches_reference_live():
     """The reference's own geodesic_segment and geodesic_raster_scan, run here
     on fresh inputs (numba's scalar typing emulated), against the oracle."""
-    if not Path("/root/reference/biomedisa/geodis.py").exists():
-        pytest.skip("reference tree not present")
     import ref_import
+
+    if not (Path(ref_import.REFERENCE_ROOT) / "biomedisa" / "geodis.py").exists():
+        pytest.skip("reference tree not present")
 
     rng = np.random.default_rng(21)
     img = rng.integers(0, 255, size=(6, 8, 7)).astype(np.uint8)
