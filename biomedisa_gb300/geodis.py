@@ -31,11 +31,13 @@ def plan_geo_labels(hist: np.ndarray):
 
 
 def _labels_for_device(labels: np.ndarray) -> np.ndarray:
-    """Integer labels in a dtype the device reads (uint8, int16, int32), with
-    every value preserved."""
+    """Integer (or boolean) labels in a dtype the device reads (uint8, int16,
+    int32), with every value preserved."""
     ld = np.dtype(labels.dtype)
     if ld in _LAB_DTYPES:
         return np.ascontiguousarray(labels)
+    if ld == np.dtype(bool):
+        return np.ascontiguousarray(labels, np.uint8)
     if not np.issubdtype(ld, np.integer):
         raise TypeError(f"geodesic_segment: integer labels expected, got {ld}")
     if ld in (np.dtype(np.int8),):

@@ -213,3 +213,41 @@ def test_plan_geo_labels():
     hist[257] = 1
     with pytest.raises(ValueError):
         plan_geo_labels(hist)
+
+
+def test_labels_for_device_preserves_values():
+    from biomedisa_gb300.geodis import _labels_for_device
+
+    rng = np.random.default_rng(1)
+    base = rng.integers(-5, 250, size=(4, 5, 6))
+    for dt, want in ((np.uint8, np.uint8), (np.int16, np.int16), (np.int32, np.int32), (np.int8, np.int16),
+                     (np.uint16, np.int32), (np.int64, np.int32), (np.uint32, np.int32), (bool, np.uint8)):
+        lab = (base > 100) if dt is bool else base.astype(dt)
+        out = _labels_for_device(lab)
+        assert out.dtype == want and out.flags.c_contiguous, dt
+        assert np.array_equal(out.astype(np.int64), lab.astype(np.int64)), dt
+    with pytest.raises(TypeError):
+        _labels_for_device(base.astype(np.float32))
+    with pytest.raises(ValueError):
+        _labels_for_device(np.full((2, 2, 2), 2 ** 40, np.int64))
+
+
+@pytest.mark.parametrize("shape", [(5, 7, 9), (40, 70, 90), (2, 3, 3), (1, 5, 5), (12, 12, 300)])
+def test_scan_launch_counts(shape):
+    """si_geo_scan_launches (host only for these modes) against the plans:
+    one launch per non-empty voxel wavefront, or per tile-wavefront."""
+    from biomedisa_gb300 import _native as nat
+
+    n = ctypes.c_longlong(0)
+    L = nat.lib()
+    waves = sum(len(np.unique(t[t >= 0])) for t in (_visit_order(shape, f) for f in (1, 0)))
+    assert L.si_geo_scan_launches(*shape, 1.0, 3, 1, ctypes.byref(n)) == 0
+    assert n.value == 3 * waves
+    assert L.si_geo_scan_launches(*shape, 0.5, 2, 4, ctypes.byref(n)) == 0
+    tile_waves = [int(_tile_order(shape, f)[0].max()) + 1 for f in (1, 0)]
+    if waves == 0:
+        assert n.value == 0
+    else:
+        assert n.value >= 2 * sum(tile_waves)
+        assert n.value <= 2 * sum(tile_waves) + 2 * 2  # a pass may end with empty tile-wavefronts
+    assert L.si_geo_scan_launches(*shape, 1.0, 1, 6, ctypes.byref(n)) != 0
