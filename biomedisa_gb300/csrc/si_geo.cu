@@ -6,9 +6,17 @@
 // voxel takes the minimum over itself and 13 neighbours that come EARLIER in
 // the pass's raster order. With t = x + 2y + 4z every one of the 13 forward
 // offsets lowers t (by 1..7) and every backward offset raises it, so all voxels
-// of one t read only finished values: one launch per wavefront t, in
-// increasing t (forward) or decreasing t (backward), reproduces the
-// sequential sweep exactly. All labels share each launch.
+// of one t read only finished values. Three schedules reproduce the
+// sequential sweep exactly:
+//   * tiled (default): tiles in skewed coordinates (p, q, r) = (t, y + 2z, z),
+//     one launch per tile-wavefront, each tile worked plane by plane in
+//     shared memory (geo_tile_kernel);
+//   * wavefronts: one launch per wavefront t, in increasing t (forward) or
+//     decreasing t (backward) (geo_wave_kernel);
+//   * cluster: every wavefront inside one launch, a thread-block cluster per
+//     label synchronised by the cluster barrier (geo_cluster_scan_kernel).
+// All labels share each launch. The tiled and wavefront launches can be
+// replayed from cached CUDA graphs.
 //
 // Arithmetic (numba's typing of the reference, see the scan kernel): the
 // intensity difference and its square are binary32, the cost sum and the
