@@ -240,3 +240,63 @@ def test_cpu_baseline_port_walks_the_reference_sample():
     except FileNotFoundError:
         pytest.skip("oracle/_ref not built here")
     assert ref[2] == port[2]
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_plan_labels_matches_reference_pre_processing_live(seed):
+    """The product's label plan (from the device histogram's 258 bins) against
+    the reference's own pre_processing (biomedisa_helper.py:639-724) on random
+    label volumes and random only/ignore strings: the label list, and for
+    every value its effective label (removed and > 255 -> 0, negatives stay
+    ignored) and slot. Negative ignore values are outside the device label map
+    and are not drawn."""
+    import types
+
+    import ref_import
+    from biomedisa_gb300 import interpolation as I
+
+    if not Path(ref_import.REFERENCE_ROOT).is_dir():
+        pytest.skip("reference tree not present")
+    rng = np.random.default_rng(seed)
+    values = rng.choice(np.arange(-3, 300), size=rng.integers(2, 9), replace=False)
+    if seed % 3 == 0:
+        values = np.append(values, 0)
+    if seed % 4 == 1:
+        values = np.append(values, -1)  # an ignored region
+    lab = rng.choice(values, size=(6, 7, 8)).astype(np.int32)
+    pos = [int(v) for v in np.unique(lab) if 0 <= v <= 255]
+    pick = lambda k: [str(v) for v in rng.choice(pos, size=min(k, len(pos)), replace=False)] if pos else []
+    only = "all" if seed % 4 == 0 else ",".join(pick(rng.integers(1, 4)) + (["77"] if seed % 5 == 0 else []))
+    ignore = "none" if seed % 3 == 1 else ",".join(pick(rng.integers(1, 3)) + (["x", "0"] if seed % 4 == 2 else []))
+    only = only or "all"
+    ignore = ignore or "none"
+    bm = types.SimpleNamespace(data=np.zeros(lab.shape, np.uint8), labelData=lab.copy(), only=only, ignore=ignore,
+                               django_env=False, success=False, process="t", path_to_data=None, path_to_labels=None,
+                               slicer=False)
+    with ref_import.reference_modules():
+        import importlib
+
+        helper = importlib.import_module("biomedisa.features.biomedisa_helper")
+        with contextlib.redirect_stdout(io.StringIO()):
+            helper.pre_processing(bm)
+    hist = np.zeros(258, np.int64)
+    for v, n in zip(*np.unique(lab, return_counts=True)):
+        hist[256 if v < 0 else 257 if v > 255 else v] += n
+    with contextlib.redirect_stdout(io.StringIO()):
+        plan = I.plan_labels(hist, only, ignore)
+    if not bm.success:  # the reference stops with fewer than two labels; the product's caller does the same
+        assert plan.nol < 2
+        return
+    assert plan.all_labels.tolist() == [int(v) for v in bm.allLabels], (only, ignore)
+    for v in np.unique(lab):
+        ref_v = np.unique(bm.labelData[lab == v])
+        assert len(ref_v) == 1
+        ref_v = int(ref_v[0])
+        if v < 0:
+            assert ref_v == v  # ignored region, kept as is
+            continue
+        eff = 0 if v > 255 else v
+        slot = int(plan.slot_lut[eff])
+        want_slot = plan.all_labels.tolist().index(ref_v) if ref_v in plan.all_labels.tolist() else -1
+        assert slot == want_slot, (int(v), ref_v, only, ignore)
+        assert bool(plan.nz_lut[eff]) == (ref_v != 0) or v > 255, (int(v), ref_v)
