@@ -40,6 +40,22 @@ def _err(message: str):
     return None
 
 
+SMOOTH_OOM_WARNING = "Warning: GPU out of memory to allocate smooth array. Process continues without smoothing."
+UNCERTAINTY_OOM_WARNING = ("Warning: GPU out of memory to allocate uncertainty array. Process continues without "
+                           "uncertainty.")
+
+
+def _or_warn_on_oom(make, warning: str):
+    """Returns make(), or None after printing ``warning`` when the device runs
+    out of memory: the reference's smoothing and uncertainty steps degrade
+    that way instead of failing the job (rw_small.py:147-149, 181-183)."""
+    try:
+        return make()
+    except torch.cuda.OutOfMemoryError:
+        print(warning)
+        return None
+
+
 def _stream() -> int:
     return torch.cuda.current_stream().cuda_stream
 
@@ -373,7 +389,10 @@ class DeviceJob:
         Z0, Y0, X0 = self.shape0
         out = torch.zeros((Z0, Y0, X0), dtype=torch.uint8, device=self.dev)
         presence = torch.zeros(8, dtype=torch.int32, device=self.dev)
-        uq = torch.zeros((Z0, Y0, X0), dtype=torch.uint8, device=self.dev) if want_uq else None
+        uq = None
+        if want_uq:
+            uq = _or_warn_on_oom(lambda: torch.zeros((Z0, Y0, X0), dtype=torch.uint8, device=self.dev),
+                                 UNCERTAINTY_OOM_WARNING)
         nat.call("si_argmax", _ptr(maps), int(is_float), self.lplan.nol, cp.Zc, cp.Yc, cp.Xc, cp.cz0, cp.cy0,
                  cp.cx0, Z0, Y0, X0, _ptr(out), _ptr(presence), _ptr(uq), _stream())
         nat.call("si_remap_labels", _ptr(out), cp.Zc, cp.Yc, cp.Xc, cp.cz0, cp.cy0, cp.cx0, Z0, Y0, X0,
@@ -422,10 +441,14 @@ class DeviceJob:
         res = self.post_regular(return_hits)
         if self.smooth:
             cp = self.cplan
-            tmp0 = torch.empty(cp.voxels, dtype=torch.float32, device=self.dev)
-            tmp1 = torch.empty(cp.voxels, dtype=torch.float32, device=self.dev)
-            self.smooth_launch(tmp0, tmp1)
-            res["smooth"] = self.post_smooth()
+            tmp = _or_warn_on_oom(lambda: (torch.empty(cp.voxels, dtype=torch.float32, device=self.dev),
+                                           torch.empty(cp.voxels, dtype=torch.float32, device=self.dev)),
+                                  SMOOTH_OOM_WARNING)
+            if tmp is None:
+                self.smooth = 0
+            else:
+                self.smooth_launch(*tmp)
+                res["smooth"] = self.post_smooth()
         return res
 
     def total_steps(self) -> int:

@@ -2,6 +2,7 @@
 slice list, volume groups of the batched walk, slot permutations of the
 surrogate's training."""
 import numpy as np
+import pytest
 
 from biomedisa_gb300 import interpolation as I
 from biomedisa_gb300.batch import volume_groups
@@ -74,3 +75,24 @@ def test_slot_permutation_keeps_slot_zero():
         new = np.arange(16)[src]
         for k in range(nol):
             assert new[3 + dst[k]] == 3 + k
+
+
+def test_out_of_memory_degrades_like_the_reference(capsys):
+    """Smoothing and uncertainty buffers: a device out-of-memory error prints
+    the reference's warning and drops that output (rw_small.py:147-149,
+    181-183); other errors propagate."""
+    import torch
+
+    def oom():
+        raise torch.cuda.OutOfMemoryError("forced")
+
+    assert I._or_warn_on_oom(oom, I.SMOOTH_OOM_WARNING) is None
+    assert capsys.readouterr().out.strip() == I.SMOOTH_OOM_WARNING
+    assert I._or_warn_on_oom(lambda: 7, I.UNCERTAINTY_OOM_WARNING) == 7
+    assert capsys.readouterr().out == ""
+
+    def other():
+        raise ValueError("not memory")
+
+    with pytest.raises(ValueError):
+        I._or_warn_on_oom(other, I.SMOOTH_OOM_WARNING)
