@@ -837,32 +837,33 @@ def run_geodesic_bench(args, wl):
     from biomedisa_gb300 import interpolation as I
 
     sys.path.insert(0, str(ROOT / "oracle"))
-    img, lab = make_inputs("geodesic")
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:  # one GPU's job; the other ranks of a multi-GPU launch exit without work
+        return
+    img, lab = make_inputs("geodesic")
     n_vox = int(np.prod(img.shape))
     nol = len(np.unique(lab[lab >= 0]))
     if args.impl == "reference":
-        if rank == 0:
-            import geo_oracle as G
+        import geo_oracle as G
 
-            times = []
-            for i in range(args.warmup + args.steps):
-                t0 = time.perf_counter()
-                G.geodesic_segment(img, lab)
-                if i >= args.warmup:
-                    times.append(time.perf_counter() - t0)
-            secs = statistics.median(times)
-            v = n_vox / secs
-            print(json.dumps({
-                "metric": "voxels/s", "value": v, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic", "impl": "reference",
-                "config": {"workload": wl["desc"], "global_batch": 1, "parallelism": "host cores"},
-                "cpu_baseline": {"value": v, "unit": "voxels/s", "cores": 1, "kind": "port",
-                                 "sample": "the whole volume; the reference's numba scan restated in C "
-                                           "(oracle/geo_oracle.c; numba is not installed), one core"},
-                "e2e": {"value": v, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        times = []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            G.geodesic_segment(img, lab)
+            if i >= args.warmup:
+                times.append(time.perf_counter() - t0)
+        secs = statistics.median(times)
+        v = n_vox / secs
+        print(json.dumps({
+            "metric": "voxels/s", "value": v, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": wl["desc"], "global_batch": 1, "parallelism": "host cores"},
+            "cpu_baseline": {"value": v, "unit": "voxels/s", "cores": 1, "kind": "port",
+                             "sample": "the whole volume; the reference's numba scan restated in C "
+                                       "(oracle/geo_oracle.c; numba is not installed), one core"},
+            "e2e": {"value": v, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
     img_t, lab_t = I.upload(img, lab)
     code_i, code_l = I._IMG_DTYPES[img.dtype], I._LAB_DTYPES[lab.dtype]
