@@ -377,7 +377,8 @@ int si_geo_masks(const void* labels, int dtype, uint64_t n,
 int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int nol,
                 double lamb, int iterations, int mode, void* stream);
 
-/* Host only (no device work): the launch plan of si_geo_scan's tiled modes
+/* No counterpart in the reference (launch-plan check).
+ * Host only (no device work): the launch plan of si_geo_scan's tiled modes
  * for the forward (fwd = 1) or backward (fwd = 0) pass: per voxel the
  * tile-wavefront (launch) wave[v], a tile id tile[v] and the plane step[v] at
  * which its CTA updates it, -1 for voxels the pass leaves alone. Fails if a
@@ -386,9 +387,11 @@ int si_geo_scan(float* c, const float* img, int Z, int Y, int X, int nol,
 int si_geo_tile_visit_order(int Z, int Y, int X, int fwd, int32_t* wave,
                             int32_t* tile, int32_t* step);
 
-/* Host only: *launches = the kernel launches one si_geo_scan call with these
- * arguments makes (1 in cluster mode, else one per non-empty wavefront and
- * iteration), after resolving mode 0 on the current device. */
+/* No counterpart in the reference (measurement).
+ * Host only: *launches = the kernel launches one si_geo_scan call with these
+ * arguments makes: 1 in cluster mode (which queries the current device), one
+ * per tile-wavefront in the tiled modes (0, 4, 5), one per non-empty
+ * wavefront in modes 1 and 3; all times `iterations` and both passes. */
 int si_geo_scan_launches(int Z, int Y, int X, double lamb, int iterations,
                          int mode, long long* launches);
 
@@ -398,7 +401,8 @@ int si_geo_scan_launches(int Z, int Y, int X, double lamb, int iterations,
 int si_geo_select(const float* c, int nol, uint64_t n,
                   const uint8_t* slot_label, uint8_t* out, void* stream);
 
-/* Host only (no device work): t_of_voxel[v] = the wavefront at which
+/* No counterpart in the reference (launch-plan checks and measurement).
+ * Host only (no device work): t_of_voxel[v] = the wavefront at which
  * si_geo_scan's forward (fwd = 1) or backward (fwd = 0) pass updates voxel v,
  * -1 for voxels the pass leaves alone. Fails if a voxel would be updated
  * twice. The launch plan of si_geo_scan, exposed for checking its order. */
