@@ -300,3 +300,42 @@ def test_plan_labels_matches_reference_pre_processing_live(seed):
         want_slot = plan.all_labels.tolist().index(ref_v) if ref_v in plan.all_labels.tolist() else -1
         assert slot == want_slot, (int(v), ref_v, only, ignore)
         assert bool(plan.nz_lut[eff]) == (ref_v != 0) or v > 255, (int(v), ref_v)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_plan_crop_matches_reference_predict_blocksize_live(seed):
+    """plan_crop (from the bounding box of nonzero pre-processed labels on
+    the padded frame, as si_slice_flags reports it) against the reference's
+    own predict_blocksize (biomedisa_helper.py:1105-1124) on random padded
+    label volumes: labels near the borders, negatives (nonzero), values > 255
+    (already 0 after pre-processing)."""
+    import types
+
+    import ref_import
+    from biomedisa_gb300 import interpolation as I
+
+    if not Path(ref_import.REFERENCE_ROOT).is_dir():
+        pytest.skip("reference tree not present")
+    rng = np.random.default_rng(100 + seed)
+    shape = tuple(int(v) for v in rng.integers(3, 260, 3))
+    lab = np.zeros(shape, np.int32)
+    for i in range(int(rng.integers(1, 4))):
+        z = int(rng.integers(0, shape[0]))
+        y0, y1 = sorted(int(v) for v in rng.integers(0, shape[1], 2))
+        x0, x1 = sorted(int(v) for v in rng.integers(0, shape[2], 2))
+        lab[z, y0:y1 + 1, x0:x1 + 1] = rng.choice([-1, 1, 2] if i == 0 else [-1, 1, 2, 300])
+    pre = np.where(lab > 255, 0, lab)  # pre_processing's > 255 rule
+    padded = np.pad(pre, 1)
+    bm = types.SimpleNamespace(labelData=padded.copy())
+    with ref_import.reference_modules():
+        import importlib
+
+        helper = importlib.import_module("biomedisa.features.biomedisa_helper")
+        helper.predict_blocksize(bm)
+    nz = np.argwhere(padded != 0)
+    bbox = (nz[:, 0].min(), nz[:, 0].max(), nz[:, 1].min(), nz[:, 1].max(), nz[:, 2].min(), nz[:, 2].max())
+    flags = [np.zeros(s + 2, np.uint8) for s in shape]
+    flags[0][np.unique(nz[:, 0])] = 1
+    cp = I.plan_crop(shape, bbox, flags, False)
+    assert (cp.cz0, cp.cz0 + cp.Zc, cp.cy0, cp.cy0 + cp.Yc, cp.cx0, cp.cx0 + cp.Xc) == (
+        bm.argmin_z, bm.argmax_z, bm.argmin_y, bm.argmax_y, bm.argmin_x, bm.argmax_x)
