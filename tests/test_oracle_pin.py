@@ -339,3 +339,45 @@ def test_plan_crop_matches_reference_predict_blocksize_live(seed):
     cp = I.plan_crop(shape, bbox, flags, False)
     assert (cp.cz0, cp.cz0 + cp.Zc, cp.cy0, cp.cy0 + cp.Yc, cp.cx0, cp.cx0 + cp.Xc) == (
         bm.argmin_z, bm.argmax_z, bm.argmin_y, bm.argmax_y, bm.argmin_x, bm.argmax_x)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_slice_readers_match_reference_live(seed):
+    """The oracle's labelled-slice readers (plain and all-axis with the
+    one-pixel-line removal) against the reference's own
+    (biomedisa_helper.py:1015-1066) on random volumes with lines, blobs and
+    labels in adjacent slices, for every axis order interpolation.py uses."""
+    import ref_import
+
+    if not Path(ref_import.REFERENCE_ROOT).is_dir():
+        pytest.skip("reference tree not present")
+    rng = np.random.default_rng(200 + seed)
+    shape = tuple(int(v) for v in rng.integers(4, 30, 3))
+    lab = np.zeros(shape, np.int32)
+    for _ in range(int(rng.integers(2, 8))):
+        ax = int(rng.integers(0, 3))
+        k = int(rng.integers(0, shape[ax]))
+        sl = [slice(None)] * 3
+        sl[ax] = k
+        plane = lab[tuple(sl)]
+        h, w = plane.shape
+        if rng.random() < 0.5:  # a one-pixel-wide line
+            r = int(rng.integers(0, h))
+            plane[r, int(rng.integers(0, w)):] = rng.choice([-1, 1, 3])
+        else:  # a blob
+            r0, c0 = int(rng.integers(0, h)), int(rng.integers(0, w))
+            plane[r0:r0 + int(rng.integers(1, 5)), c0:c0 + int(rng.integers(1, 5))] = rng.choice([1, 2, 7])
+    with ref_import.reference_modules():
+        import importlib
+
+        helper = importlib.import_module("biomedisa.features.biomedisa_helper")
+        arrays = [lab, np.ascontiguousarray(np.swapaxes(lab, 0, 1)),
+                  np.ascontiguousarray(np.swapaxes(np.swapaxes(lab, 0, 1), 0, 2))]
+        for ax, arr in enumerate(arrays):
+            ri, rd = helper.read_labeled_slices(arr.copy())
+            oi, od = O.read_labeled_slices(arr)
+            assert list(ri) == list(oi) and np.array_equal(rd, od)
+            ri, rd = helper.read_labeled_slices_allx(arr.copy(), ax)
+            oi, od = O.read_labeled_slices_allx(arr, ax)
+            assert list(ri) == list(oi) and np.array_equal(rd, od), (seed, ax)
+            assert list(helper.read_indices_allx(arr.copy(), ax)) == list(O.read_indices_allx(arr, ax))
