@@ -381,3 +381,30 @@ def test_slice_readers_match_reference_live(seed):
             oi, od = O.read_labeled_slices_allx(arr, ax)
             assert list(ri) == list(oi) and np.array_equal(rd, od), (seed, ax)
             assert list(helper.read_indices_allx(arr.copy(), ax)) == list(O.read_indices_allx(arr, ax))
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_get_labels_and_denoise_match_reference_live(seed):
+    """get_labels (biomedisa_helper.py:1209-1213; the smallest index present
+    keeps 0) and the 3x3x3 denoise smooth_img_3x3 (:308-323, run with numba's
+    accumulator typing) of the reference against the oracle's, on random
+    inputs (uint8 and float32 images, the dtypes denoise sees)."""
+    import ref_import
+
+    if not Path(ref_import.REFERENCE_ROOT).is_dir():
+        pytest.skip("reference tree not present")
+    rng = np.random.default_rng(300 + seed)
+    pre = rng.integers(seed % 2, 5, size=(7, 8, 9)).astype(np.uint8)  # index 0 present or absent
+    labels = np.asarray(sorted(rng.choice(np.arange(1, 200), size=5, replace=False)))
+    img8 = rng.integers(0, 256, size=(6, 7, 9)).astype(np.uint8)
+    imgf = (rng.random((5, 8, 6)) * 255).astype(np.float32)
+    with ref_import.reference_modules():
+        import importlib
+
+        helper = importlib.import_module("biomedisa.features.biomedisa_helper")
+        ref_gl = helper.get_labels(pre.copy(), labels)
+        ref_d8 = helper.smooth_img_3x3(img8.copy())
+        ref_df = helper.smooth_img_3x3(imgf.copy())
+    assert np.array_equal(O.get_labels(pre, labels), ref_gl)
+    assert np.array_equal(O.smooth_img_3x3(img8), ref_d8)
+    assert np.array_equal(O.smooth_img_3x3(imgf).view(np.uint32), ref_df.view(np.uint32))
