@@ -408,3 +408,34 @@ def test_get_labels_and_denoise_match_reference_live(seed):
     assert np.array_equal(O.get_labels(pre, labels), ref_gl)
     assert np.array_equal(O.smooth_img_3x3(img8), ref_d8)
     assert np.array_equal(O.smooth_img_3x3(imgf).view(np.uint32), ref_df.view(np.uint32))
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_smoothing_matches_reference_kernels_live(seed):
+    """Curvature smoothing: the reference's own curvature and update kernels
+    (gpu_kernels.py:118-183, compiled as C under oracle/_ref, launched with
+    rw_small.py's grid) on random maps, iterated, against the oracle's
+    smooth(update='ref_f64'), bit for bit."""
+    import ctypes
+
+    import ref_run
+
+    try:
+        lib = ref_run.ref_lib()
+    except FileNotFoundError:
+        pytest.skip("oracle/_ref not built here")
+    rng = np.random.default_rng(400 + seed)
+    Z, Y, X = (int(v) for v in rng.integers(5, 40, 3))
+    phi = (rng.random((Z, Y, X)) * 50).astype(np.float32)
+    phi[rng.random(phi.shape) < 0.3] = 0.0  # hit maps hold many zeros
+    iters = int(rng.integers(1, 6))
+    want = O.smooth(phi[None], iters, update="ref_f64")[0]
+    a = np.ascontiguousarray(phi.copy())
+    b = np.zeros_like(a)
+    grid = (X // 32 + 1, Y // 32 + 1, Z)  # rw_small.py:104-108
+    p = [v.ctypes.data_as(ctypes.c_void_p) for v in (a, b)]
+    for _ in range(iters):
+        for kind in (0, 1):  # curvature, then update
+            lib.ref_launch_post(ctypes.c_int(kind), *map(ctypes.c_int, grid), *p, ctypes.c_int(X), ctypes.c_int(Y))
+    assert not np.array_equal(a, phi)  # the kernels did run
+    assert np.array_equal(a.view(np.uint32), want.view(np.uint32))
