@@ -439,3 +439,39 @@ def test_smoothing_matches_reference_kernels_live(seed):
             lib.ref_launch_post(ctypes.c_int(kind), *map(ctypes.c_int, grid), *p, ctypes.c_int(X), ctypes.c_int(Y))
     assert not np.array_equal(a, phi)  # the kernels did run
     assert np.array_equal(a.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_uncertainty_matches_reference_kernels_live(seed):
+    """Uncertainty: the reference's max and uncertainty kernels
+    (gpu_kernels.py:54-116, compiled as C under oracle/_ref) run as
+    rw_small.py:152-176 does (max over the labels' maps, then uncertainty,
+    then uint8(uq * 255)) on random hit maps with ties and a zero border,
+    against the oracle's uncertainty()."""
+    import ctypes
+
+    import ref_run
+
+    try:
+        lib = ref_run.ref_lib()
+    except FileNotFoundError:
+        pytest.skip("oracle/_ref not built here")
+    rng = np.random.default_rng(500 + seed)
+    nol = int(rng.integers(2, 6))
+    Z, Y, X = (int(v) for v in rng.integers(4, 30, 3))
+    maps = rng.integers(0, 6, size=(nol, Z, Y, X)).astype(np.float32)  # small counts: many ties and zeros
+    maps[:, [0, -1]] = 0
+    maps[:, :, [0, -1]] = 0
+    maps[:, :, :, [0, -1]] = 0
+    grid = (X // 32 + 1, Y // 32 + 1, Z)
+    mx = np.zeros((3, Z, Y, X), np.float32)
+    a = None
+    for k in range(nol):
+        a = np.ascontiguousarray(maps[k].copy())
+        lib.ref_launch_post(ctypes.c_int(2), *map(ctypes.c_int, grid), mx.ctypes.data_as(ctypes.c_void_p),
+                            a.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(X), ctypes.c_int(Y))
+    lib.ref_launch_post(ctypes.c_int(3), *map(ctypes.c_int, grid), mx.ctypes.data_as(ctypes.c_void_p),
+                        a.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(X), ctypes.c_int(Y))
+    ref = (a * 255.0).astype(np.uint8)
+    assert ref.any()
+    assert np.array_equal(O.uncertainty(maps), ref)
