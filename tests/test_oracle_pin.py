@@ -475,3 +475,39 @@ def test_uncertainty_matches_reference_kernels_live(seed):
     ref = (a * 255.0).astype(np.uint8)
     assert ref.any()
     assert np.array_equal(O.uncertainty(maps), ref)
+
+
+@pytest.mark.skipif(not _ref_available(), reason="oracle/_ref (reference kernels compiled as C) not built")
+@pytest.mark.parametrize("seed", [31, 32])
+def test_oracle_reference_mode_matches_reference_float_kernel_live(seed):
+    """The reference CUDA walker's float32-image kernel (pycuda_small.py:
+    264-410, taken by every non-uint8 input) compiled as C, on a uint16
+    volume normalised as interpolation.py:136-144 does, vs the oracle in
+    reference mode."""
+    import ctypes
+
+    import ref_run
+    from biomedisa_gb300.synthetic import plain_volume
+
+    img, lab, _ = plain_volume(seed=seed, shape=(24, 28, 26), z_every=4, semi=(4, 9))
+    img16 = (img.astype(np.uint16) * 211 + 7).astype(np.uint16)
+    data = np.pad(O.normalize_image(img16), 1)
+    assert data.dtype == np.float32
+    l2 = np.pad(lab, 1)
+    _, all_labels = O.pre_processing(l2)
+    idx, stack = O.read_labeled_slices(l2)
+    seeds = O.extract_seeds(data, l2, [(0, k) for k in idx], all_labels)
+    hits = O.walk_c(data, seeds, 2, 40, 0, len(all_labels), rng="ref_mrg", weight="ref_expf",
+                    rng_index=seeds.rng_cuda)
+    assert hits.sum() > 0
+    lib = ref_run.ref_lib()
+    raw = np.ascontiguousarray(data, np.float32)
+    Z, Y, X = data.shape
+    ind = np.asarray(idx, np.int32)
+    st = np.ascontiguousarray(stack, np.int32)
+    for s, seg in enumerate(all_labels):
+        a = np.zeros((Z, Y, X), np.float32)
+        lib.ref_launch_walk(1, X // 32 + 1, Y // 32 + 1, len(idx), int(seg), raw.ctypes.data_as(ctypes.c_void_p),
+                            st.ctypes.data_as(ctypes.c_void_p), a.ctypes.data_as(ctypes.c_void_p), X, Y, Z,
+                            ind.ctypes.data_as(ctypes.c_void_p), 40, 2)
+        assert np.array_equal(a, hits[s].astype(np.float32)), f"label {seg}"
