@@ -511,3 +511,35 @@ def test_oracle_reference_mode_matches_reference_float_kernel_live(seed):
                             st.ctypes.data_as(ctypes.c_void_p), a.ctypes.data_as(ctypes.c_void_p), X, Y, Z,
                             ind.ctypes.data_as(ctypes.c_void_p), 40, 2)
         assert np.array_equal(a, hits[s].astype(np.float32)), f"label {seg}"
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_cc_oracle_matches_reference_clean_fill_live(seed):
+    """oracle/cc_oracle.py against the reference's own clean() and fill()
+    (remove_outlier.py:45-141) run here on random label volumes: phases with
+    speckle and holes."""
+    import cc_oracle as C
+    import ref_import
+    from biomedisa_gb300 import synthetic as S
+
+    if not Path(ref_import.REFERENCE_ROOT).is_dir():
+        pytest.skip("reference tree not present")
+    rng = np.random.default_rng(600 + seed)
+    shape = tuple(int(v) for v in rng.integers(10, 26, 3))
+    truth = np.zeros(shape, np.uint8)
+    S._phases(rng, truth, int(rng.integers(2, 5)), size_frac=(0.2, 0.4))
+    vol = truth.copy()
+    sel = rng.random(shape) < 0.03
+    vol[sel] = rng.integers(0, 5, size=int(sel.sum()))
+    with ref_import.reference_modules():
+        import importlib
+
+        ro = importlib.import_module("biomedisa.features.remove_outlier")
+        for thr in (0.1, 0.6):
+            assert np.array_equal(C.clean(vol, thr), ro.clean(vol.copy(), thr)), thr
+        for thr in (0.9, 0.4):
+            try:
+                want = ro.fill(vol.copy(), thr)
+            except ValueError:
+                continue  # a label vanished under filling: the reference raises (the product skips it)
+            assert np.array_equal(C.fill(vol, thr), want), thr
