@@ -112,6 +112,11 @@ def geodesic_raster_scan(img, c, lamb=1.0, iterations=4):
 def geodesic_segment_device(img: torch.Tensor, img_dtype: int, lab: torch.Tensor, lab_dtype: int) -> torch.Tensor:
     """geodesic_segment on device-resident (Z, Y, X) tensors of the given
     si_dtype codes; returns the uint8 label volume on the device."""
+    if img.dim() != 3 or tuple(lab.shape) != tuple(img.shape):
+        raise ValueError("geodesic_segment_device: image and labels must be 3-D volumes of one shape")
+    if not (img.is_cuda and lab.is_cuda) or img.device != lab.device or not (img.is_contiguous() and
+                                                                              lab.is_contiguous()):
+        raise ValueError("geodesic_segment_device: contiguous tensors on one CUDA device expected")
     Z, Y, X = img.shape
     n = Z * Y * X
     dev = img.device

@@ -242,6 +242,8 @@ class DeviceJob:
         self.walker = walker
         if img.dim() != 3 or lab.dim() != 3 or tuple(img.shape) != tuple(lab.shape):
             raise ValueError("image and labels must be 3-D volumes of the same shape")
+        if not (img.is_cuda and lab.is_cuda) or img.device != lab.device:
+            raise ValueError("image and labels must be tensors on one CUDA device")
         self.img, self.img_code, self.lab, self.lab_code = img, img_code, lab, lab_code
         self.shape0 = tuple(int(s) for s in img.shape)
         self.nbrw, self.sorw = int(nbrw), int(sorw)

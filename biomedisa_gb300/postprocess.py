@@ -29,8 +29,8 @@ def present_labels(labels: torch.Tensor) -> list[int]:
 
 def clean(labels: torch.Tensor, threshold: float = 0.1) -> torch.Tensor:
     """remove_outlier.clean on a uint8 device volume; returns a new volume."""
-    if labels.dtype != torch.uint8 or labels.dim() != 3:
-        raise ValueError("clean takes a 3-D uint8 label volume")
+    if labels.dtype != torch.uint8 or labels.dim() != 3 or not labels.is_cuda:
+        raise ValueError("clean takes a 3-D uint8 label volume on a CUDA device")
     labels = labels.contiguous()
     present = present_labels(labels)
     skip = present[0] if present else -1
@@ -43,8 +43,8 @@ def clean(labels: torch.Tensor, threshold: float = 0.1) -> torch.Tensor:
 
 def fill(labels: torch.Tensor, threshold: float = 0.9) -> torch.Tensor:
     """remove_outlier.fill on a uint8 device volume; returns a new volume."""
-    if labels.dtype != torch.uint8 or labels.dim() != 3:
-        raise ValueError("fill takes a 3-D uint8 label volume")
+    if labels.dtype != torch.uint8 or labels.dim() != 3 or not labels.is_cuda:
+        raise ValueError("fill takes a 3-D uint8 label volume on a CUDA device")
     out = labels.contiguous().clone()
     todo = present_labels(out)[1:]
     if not todo:

@@ -64,3 +64,55 @@ def test_binding_arities_match_header():
     assert set(_native._SIGNATURES) <= set(ar)
     for name, args in _native._SIGNATURES.items():
         assert len(args) == ar[name], (name, len(args), ar[name])
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    """Without libsmartinterp.so the binding raises: there is no CPU fallback."""
+    import pytest
+
+    from biomedisa_gb300 import _native
+
+    with pytest.raises(ImportError, match="no CPU fallback"):
+        _native.load(tmp_path / "libsmartinterp.so")
+
+
+def test_entry_points_need_a_device_without_cuda():
+    """On a host without a CUDA device the public calls raise instead of
+    computing on the CPU."""
+    import numpy as np
+    import pytest
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    from biomedisa_gb300 import geodis, smart_interpolation
+
+    img = np.zeros((4, 5, 6), np.uint8)
+    lab = np.zeros(img.shape, np.int32)
+    lab[1, 1:3, 1:3] = 1
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        smart_interpolation(img, lab)
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        geodis.geodesic_segment(img, lab)
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        geodis.geodesic_raster_scan(img.astype(np.float32), np.zeros(img.shape, np.float32))
+
+
+def test_device_tensor_apis_refuse_host_tensors():
+    """Entry points that take device tensors refuse host tensors before any
+    kernel could be handed a host pointer."""
+    import pytest
+    import torch
+
+    from biomedisa_gb300 import geodis, interpolation, postprocess
+
+    lab8 = torch.zeros((4, 5, 6), dtype=torch.uint8)
+    for fn in (postprocess.clean, postprocess.fill):
+        with pytest.raises(ValueError, match="CUDA"):
+            fn(lab8, 0.5)
+    img = torch.zeros((4, 5, 6), dtype=torch.uint8)
+    lab = torch.zeros((4, 5, 6), dtype=torch.int32)
+    with pytest.raises(ValueError, match="CUDA"):
+        interpolation.DeviceJob(img, 0, lab, 4)
+    with pytest.raises(ValueError, match="CUDA"):
+        geodis.geodesic_segment_device(img, 0, lab, 4)
