@@ -73,8 +73,8 @@ def scan_device(c: torch.Tensor, img: torch.Tensor, lamb: float = 1.0, iteration
         raise TypeError("scan_device: float32 CUDA tensors expected")
     if img.dim() != 3 or tuple(c.shape[-3:]) != tuple(img.shape) or c.dim() not in (3, 4):
         raise ValueError("scan_device: c must be (Z, Y, X) or (nol, Z, Y, X) over img's shape")
-    if not (c.is_contiguous() and img.is_contiguous()):
-        raise ValueError("scan_device: tensors must be contiguous")
+    if not (c.is_contiguous() and img.is_contiguous()) or c.device != img.device:
+        raise ValueError("scan_device: contiguous tensors on one device expected")
     Z, Y, X = img.shape
     nol = 1 if c.dim() == 3 else c.shape[0]
     if nol:
