@@ -19,6 +19,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -493,7 +494,10 @@ BrickGeom make_geom(int Zc, int Yc, int Xc, int edge = kCore) {
 }
 
 int advance_blocks_per_sm() {
-  static int cached = 0;
+  static std::atomic<int> cached_dev[64];  // per device (the shared-memory opt-in is per device); 0 = not yet set
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  int cached = cached_dev[dev].load(std::memory_order_acquire);
   if (!cached) {
     const int smem = kExtVox * (int)(sizeof(uint2) + sizeof(uint32_t));
     cudaFuncSetAttribute(brick_advance_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -502,6 +506,7 @@ int advance_blocks_per_sm() {
         n < 1)
       n = 1;
     cached = n;
+    cached_dev[dev].store(n, std::memory_order_release);
   }
   return cached;
 }

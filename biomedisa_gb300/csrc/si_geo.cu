@@ -21,6 +21,7 @@
 // Arithmetic (numba's typing of the reference, see the scan kernel): the
 // intensity difference and its square are binary32, the cost sum and the
 // comparison binary64, the store rounds to binary32.
+#include <atomic>
 #include <cmath>
 #include <mutex>
 #include <vector>
@@ -526,11 +527,11 @@ namespace {
 // Clusters of the scan kernel that fit on the current device at once (0 if
 // the cluster launch is not possible), cached per device.
 int geo_cluster_capacity(bool lamb1) {
-  static int cache[2][64];
-  static bool known[2][64];
+  static std::atomic<int> cache[2][64];  // capacity + 1; 0 = not yet queried
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-  if (known[lamb1][dev]) return cache[lamb1][dev];
+  const int known = cache[lamb1][dev].load(std::memory_order_relaxed);
+  if (known) return known - 1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(kGeoCluster);
   cfg.blockDim = dim3(kGeoClusterThreads);
@@ -549,8 +550,7 @@ int geo_cluster_capacity(bool lamb1) {
     (void)cudaGetLastError();
     n = 0;
   }
-  cache[lamb1][dev] = n;
-  known[lamb1][dev] = true;
+  cache[lamb1][dev].store(n + 1, std::memory_order_relaxed);
   return n;
 }
 
@@ -582,16 +582,16 @@ int geo_resolve_mode(int Z, int Y, int X, bool lamb1, int mode, bool* cluster) {
 
 // Opt-in shared memory of the tiled kernel (once per device, outside any capture).
 int geo_tile_prepare() {
-  static bool done[64];
+  static std::atomic<bool> done[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return check_launch("si_geo_scan (device)");
-  if (done[dev]) return SI_OK;
+  if (done[dev].load(std::memory_order_acquire)) return SI_OK;
   if (cudaFuncSetAttribute(geo_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem) !=
           cudaSuccess ||
       cudaFuncSetAttribute(geo_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem) !=
           cudaSuccess)
     return check_launch("si_geo_scan (tile shared memory)");
-  done[dev] = true;
+  done[dev].store(true, std::memory_order_release);
   return SI_OK;
 }
 
