@@ -45,11 +45,16 @@ def _load() -> dict:
 
 
 def _store(key: str, value) -> None:
+    """Adds one entry; the file is replaced atomically, so a concurrent reader
+    sees the old or the new cache, never a partial one."""
     data = _load()
     data[key] = value
+    path = cache_path()
     try:
-        cache_path().parent.mkdir(parents=True, exist_ok=True)
-        cache_path().write_text(json.dumps(data, indent=1))
+        path.parent.mkdir(parents=True, exist_ok=True)
+        tmp = path.with_name(f"{path.name}.{os.getpid()}.tmp")
+        tmp.write_text(json.dumps(data, indent=1))
+        os.replace(tmp, path)
     except OSError:
         pass
 

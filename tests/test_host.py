@@ -96,3 +96,16 @@ def test_out_of_memory_degrades_like_the_reference(capsys):
 
     with pytest.raises(ValueError):
         I._or_warn_on_oom(other, I.SMOOTH_OOM_WARNING)
+
+
+def test_autotune_cache_round_trip(tmp_path, monkeypatch):
+    from biomedisa_gb300 import autotune as A
+
+    monkeypatch.setenv("SI_AUTOTUNE_CACHE", str(tmp_path / "sub" / "tune.json"))
+    assert A._load() == {}
+    A._store("k1", [6, 32])
+    A._store("k2", [8, 64])
+    assert A._load() == {"k1": [6, 32], "k2": [8, 64]}
+    assert sorted(p.name for p in (tmp_path / "sub").iterdir()) == ["tune.json"]  # no temporary left behind
+    (tmp_path / "sub" / "tune.json").write_text("{not json")
+    assert A._load() == {}  # a damaged cache is ignored (the workload is tuned again)
