@@ -214,15 +214,30 @@ class SurrogateNet:
         return loss / denom, dl
 
     # ---- persistence --------------------------------------------------------
+    _MOMENTS = ("mw", "vw", "mb", "vb")
+
     def state_dict(self):
-        return {"channels": self.channels, "dilations": list(self.dilations), "step": self.step_count,
-                "w": [c.w.cpu() for c in self.convs], "b": [c.b.cpu() for c in self.convs]}
+        """Checkpoint: fp32 weights and biases, the AdamW moments and the step
+        count (AdamW's bias correction), so training can resume where it
+        stopped."""
+        sd = {"channels": self.channels, "dilations": list(self.dilations), "step": self.step_count,
+              "w": [c.w.cpu() for c in self.convs], "b": [c.b.cpu() for c in self.convs]}
+        for m in self._MOMENTS:
+            sd[m] = [getattr(c, m).cpu() for c in self.convs]
+        return sd
 
     def load_state_dict(self, sd):
-        for c, w, b in zip(self.convs, sd["w"], sd["b"]):
+        """Loads a checkpoint; one without moments (weights only) restarts them at zero."""
+        if len(sd["w"]) != len(self.convs):
+            raise ValueError("checkpoint of a different network depth")
+        for i, (c, w, b) in enumerate(zip(self.convs, sd["w"], sd["b"])):
+            if tuple(w.shape) != tuple(c.w.shape) or tuple(b.shape) != tuple(c.b.shape):
+                raise ValueError("checkpoint of a different network shape")
             c.w.copy_(w.to(self.device))
             c.b.copy_(b.to(self.device))
             c.wb.copy_(c.w.to(BF16))
+            for m in self._MOMENTS:
+                getattr(c, m).copy_(sd[m][i].to(self.device) if m in sd else torch.zeros_like(getattr(c, m)))
         self.step_count = int(sd.get("step", 0))
 
 

@@ -109,3 +109,35 @@ def test_autotune_cache_round_trip(tmp_path, monkeypatch):
     assert sorted(p.name for p in (tmp_path / "sub").iterdir()) == ["tune.json"]  # no temporary left behind
     (tmp_path / "sub" / "tune.json").write_text("{not json")
     assert A._load() == {}  # a damaged cache is ignored (the workload is tuned again)
+
+
+def test_surrogate_checkpoint_round_trip(tmp_path):
+    """save/load keep weights, biases, AdamW moments and the step count; a
+    weights-only checkpoint loads with zero moments; a different shape is
+    refused. (The network is built on the CPU device here: no kernel runs.)"""
+    import torch
+
+    from biomedisa_gb300 import surrogate as SG
+
+    a = SG.SurrogateNet(device="cpu", seed=1)
+    g = torch.Generator().manual_seed(5)
+    for c in a.convs:
+        for m in ("mw", "vw", "mb", "vb"):
+            getattr(c, m).copy_(torch.rand(getattr(c, m).shape, generator=g))
+    a.step_count = 17
+    path = tmp_path / "net.pt"
+    SG.save(a, path)
+    b = SG.load(path, device="cpu")
+    assert b.step_count == 17 and (b.channels, b.dilations) == (a.channels, a.dilations)
+    for ca, cb in zip(a.convs, b.convs):
+        for f in ("w", "b", "wb", "mw", "vw", "mb", "vb"):
+            assert torch.equal(getattr(ca, f), getattr(cb, f)), f
+    sd = a.state_dict()
+    for m in ("mw", "vw", "mb", "vb"):
+        del sd[m]
+    c = SG.SurrogateNet(device="cpu", seed=2)
+    c.load_state_dict(sd)
+    assert torch.equal(c.convs[3].w, a.convs[3].w) and not c.convs[3].mw.any()
+    d = SG.SurrogateNet(channels=32, device="cpu")
+    with pytest.raises(ValueError):
+        d.load_state_dict(a.state_dict())
