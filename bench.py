@@ -425,7 +425,7 @@ def main():
     line = {
         "metric": "walker-steps/s", "value": value, "unit": "walker-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u8", "data": "synthetic (seeded generator, no public dataset)",
+        "dtype": "f32", "data": "synthetic (seeded generator, no public dataset)",
         "config": {"workload": wl["desc"], "global_batch": 1, "parallelism": f"replicas x{world}" if world > 1
                    else "single GPU", "l2": "256 MiB buffer written before every timed step; hit maps 3.8 GB > L2"},
         "voxels_per_s": world * int(np.prod(img.shape)) / (ms / 1e3),
@@ -433,19 +433,20 @@ def main():
         "e2e": {"value": e2e_value, "unit": "walker-steps/s", "seconds": e2e_s,
                 "h2d_bytes_per_step": int(img.nbytes + lab.nbytes), "d2h_bytes_per_step": int(out_bytes)},
         "gpu_launches": launches // max(args.steps, 1),
-        "roofline": {"bound": "hbm", "achieved": achieved_payload, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved_payload / hbm, "traffic": traffic,
-                     "note": f"walker (sweep_kernel, {sweeps} launches per job); algorithmic bytes = "
-                             f"{WALK_BYTES_PAYLOAD_U8} B/step logical payload (6 neighbour bytes + 4-byte hit) x "
-                             f"steps / CUDA-event walk duration; peak {peak_kind} (MEASURED_PEAKS.json hbm_gbs); "
-                             "traffic = DRAM bytes per sweep launch from profiles/sweep_kernel_allaxis.md "
-                             f"({traffic_per_step} B/step, scaled by steps per launch)"},
-        "roofline_l2": {"bound": "l2", "achieved": achieved_l2, "peak": l2_gbs, "unit": "GB/s",
-                        "frac": achieved_l2 / l2_gbs if l2_gbs else None,
-                        "atomics_per_s": walk_rate, "atomic_peak_per_s": l2["atomics_per_s"],
-                        "note": f"walker: {WALK_SECTORS_L2} x 32 B sectors per step at L2 (one packed "
-                                "neighbourhood record + one hit atomic); peak = si_probe_l2_read over a 48 MiB "
-                                "L2-resident buffer measured in this run; atomic peak = si_probe_l2_atomics"},
+        "roofline": {"bound": "l2", "achieved": achieved_l2, "peak": l2_gbs, "unit": "GB/s",
+                     "frac": achieved_l2 / l2_gbs if l2_gbs else None, "traffic": traffic,
+                     "atomics_per_s": walk_rate, "atomic_peak_per_s": l2["atomics_per_s"],
+                     "note": f"walker (sweep_kernel, {sweeps} launches per job), issue- and L2-bound: "
+                             f"{WALK_SECTORS_L2} x 32 B sectors per step at L2 (one packed neighbourhood record "
+                             "+ one hit atomic) x steps / CUDA-event walk duration; peak = L2 read ceiling "
+                             "measured in this run by si_probe_l2_read over a 48 MiB L2-resident buffer (no L2 "
+                             "figure in the measured-peaks file); atomic peak = si_probe_l2_atomics; traffic = "
+                             f"DRAM bytes per sweep launch from the committed ncu summary ({traffic_per_step} "
+                             "B/step, scaled by steps per launch)"},
+        "roofline_hbm": {"bound": "hbm", "achieved": achieved_payload, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved_payload / hbm,
+                         "note": f"walker logical payload {WALK_BYTES_PAYLOAD_U8} B/step (6 neighbour bytes + "
+                                 f"4-byte hit) against HBM; peak {peak_kind} (hbm_gbs)"},
         "clocks": clocks.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:

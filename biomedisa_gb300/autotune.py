@@ -14,6 +14,8 @@ import ctypes
 import json
 import math
 import os
+import tempfile
+import threading
 from pathlib import Path
 
 import torch
@@ -44,19 +46,35 @@ def _load() -> dict:
         return {}
 
 
+_STORE_LOCK = threading.Lock()
+
+
 def _store(key: str, value) -> None:
     """Adds one entry; the file is replaced atomically, so a concurrent reader
-    sees the old or the new cache, never a partial one."""
-    data = _load()
-    data[key] = value
-    path = cache_path()
-    try:
-        path.parent.mkdir(parents=True, exist_ok=True)
-        tmp = path.with_name(f"{path.name}.{os.getpid()}.tmp")
-        tmp.write_text(json.dumps(data, indent=1))
-        os.replace(tmp, path)
-    except OSError:
-        pass
+    sees the old or the new cache, never a partial one. Threads of one process
+    take turns (the read-modify-write keeps every thread's entry), and each
+    write goes through its own uniquely named temporary file."""
+    with _STORE_LOCK:
+        data = _load()
+        data[key] = value
+        path = cache_path()
+        tmp = None
+        try:
+            path.parent.mkdir(parents=True, exist_ok=True)
+            with tempfile.NamedTemporaryFile("w", dir=path.parent, prefix=path.name + ".", suffix=".tmp",
+                                             delete=False) as f:
+                tmp = f.name
+                f.write(json.dumps(data, indent=1))
+            os.replace(tmp, path)
+            tmp = None
+        except OSError:
+            pass
+        finally:
+            if tmp is not None:
+                try:
+                    os.unlink(tmp)
+                except OSError:
+                    pass
 
 
 def tune(vol_array, n_vols: int, hits: list, nbrw: int, sorw: int, key: int, walks: int, use_cache: bool = True):

@@ -23,6 +23,8 @@ NVCC_FLAGS = [
     "-lineinfo",
     "-std=c++17",
     "--fmad=false",  # no implicit contraction: fused ops only where written
+    "-Xptxas",
+    "--fmad=false",  # nor in ptxas (packed .f32x2 products feeding packed sums)
     "-Xcompiler",
     "-fPIC",
     "-Xptxas",

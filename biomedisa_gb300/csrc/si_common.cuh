@@ -83,6 +83,73 @@ __device__ __forceinline__ float edge_weight(float d2, float c) {
   return __int_as_float(__float_as_int(p) - (k << 23));
 }
 
+// ---------------------------------------------------------------------------
+// Two edge weights at once on the packed binary32 pipe of sm_100-class SMs
+// (add/sub/mul/fma.rn.f32x2: one instruction, two independent IEEE-754
+// round-to-nearest results). Each lane performs exactly the operation sequence
+// of edge_weight() above, so the pair equals two scalar calls bit for bit (the
+// library is built with ptxas contraction off, so a packed product is never
+// fused into a following packed sum). The walker is issue-bound and this
+// halves the floating-point instructions of its six weights. Operands travel
+// as 64-bit registers {lo, hi}.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ void u2_unpack(uint64_t v, uint32_t& lo, uint32_t& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_splat(float v) { return f2_pack(v, v); }
+
+// Weights of the two neighbours whose (B - I) differences are the lanes of d;
+// cc = {c, c}. Returns w_lo, w_hi equal to edge_weight(d_lo^2, c) and
+// edge_weight(d_hi^2, c).
+__device__ __forceinline__ void edge_weight_pair(uint64_t d, uint64_t cc, float& w_lo, float& w_hi) {
+  const uint64_t magic2 = f2_splat(kRoundMagic);
+  const uint64_t y = f2_mul(f2_mul(d, d), cc);
+  const uint64_t r = f2_add(y, magic2);
+  const uint64_t g = f2_sub(f2_sub(r, magic2), y);
+  uint64_t p = f2_fma(f2_splat(kP5), g, f2_splat(kP4));
+  p = f2_fma(p, g, f2_splat(kP3));
+  p = f2_fma(p, g, f2_splat(kP2));
+  p = f2_fma(p, g, f2_splat(kP1));
+  p = f2_fma(p, g, f2_splat(1.0f));
+  uint32_t p_lo, p_hi, r_lo, r_hi;
+  u2_unpack(p, p_lo, p_hi);
+  u2_unpack(r, r_lo, r_hi);
+  float y_lo, y_hi;
+  f2_unpack(y, y_lo, y_hi);
+  // 2^-k through the exponent field: k = bits(r) - bits(1.5*2^23), and
+  // (bits(1.5*2^23) << 23) vanishes modulo 2^32, so k << 23 == bits(r) << 23.
+  w_lo = y_lo < kWeightYMax ? __uint_as_float(p_lo - (r_lo << 23)) : 0.0f;
+  w_hi = y_hi < kWeightYMax ? __uint_as_float(p_hi - (r_hi << 23)) : 0.0f;
+}
+
 // Per-seed weight constant c = RN(RN(1 / RN(2 var)) * log2e).
 __device__ __forceinline__ float weight_constant(float var) {
   const float div1 = __fdiv_rn(1.0f, __fmul_rn(2.0f, var));
@@ -122,26 +189,24 @@ __device__ __forceinline__ uint32_t walk_step(const void* __restrict__ packed_v,
                                               const int32_t* s_delta) {
   float w0, w1, w2, w3, w4, w5;
   uint32_t mask;
+  // The (B - I) differences are formed pairwise (+z,-z), (+y,-y), (+x,-x) and
+  // weighted on the packed pipe; d = B - I is exact in both record kinds
+  // (uint8: (2^23 + B) - (2^23 + I); float: one RN subtraction, as before).
+  const uint64_t cc = f2_splat(c);
   if (kFloat) {
     const float4* rec = static_cast<const float4*>(packed_v) + 2 * (size_t)pos;
     const float4 a = rec[0], b = rec[1];
-    float d;
-    d = __fsub_rn(bf, a.x); w0 = edge_weight(__fmul_rn(d, d), c);
-    d = __fsub_rn(bf, a.y); w1 = edge_weight(__fmul_rn(d, d), c);
-    d = __fsub_rn(bf, a.z); w2 = edge_weight(__fmul_rn(d, d), c);
-    d = __fsub_rn(bf, a.w); w3 = edge_weight(__fmul_rn(d, d), c);
-    d = __fsub_rn(bf, b.x); w4 = edge_weight(__fmul_rn(d, d), c);
-    d = __fsub_rn(bf, b.y); w5 = edge_weight(__fmul_rn(d, d), c);
+    const uint64_t bf2 = f2_splat(bf);
+    edge_weight_pair(f2_sub(bf2, f2_pack(a.x, a.y)), cc, w0, w1);
+    edge_weight_pair(f2_sub(bf2, f2_pack(a.z, a.w)), cc, w2, w3);
+    edge_weight_pair(f2_sub(bf2, f2_pack(b.x, b.y)), cc, w4, w5);
     mask = __float_as_uint(b.z);
   } else {
     const uint2 r = static_cast<const uint2*>(packed_v)[pos];
-    float d;
-    d = __fsub_rn(b23, byte_plus_2p23(r.x, 0)); w0 = edge_weight(__fmul_rn(d, d), c);
-    d = __fsub_rn(b23, byte_plus_2p23(r.x, 1)); w1 = edge_weight(__fmul_rn(d, d), c);
-    d = __fsub_rn(b23, byte_plus_2p23(r.x, 2)); w2 = edge_weight(__fmul_rn(d, d), c);
-    d = __fsub_rn(b23, byte_plus_2p23(r.x, 3)); w3 = edge_weight(__fmul_rn(d, d), c);
-    d = __fsub_rn(b23, byte_plus_2p23(r.y, 0)); w4 = edge_weight(__fmul_rn(d, d), c);
-    d = __fsub_rn(b23, byte_plus_2p23(r.y, 1)); w5 = edge_weight(__fmul_rn(d, d), c);
+    const uint64_t b2 = f2_splat(b23);
+    edge_weight_pair(f2_sub(b2, f2_pack(byte_plus_2p23(r.x, 0), byte_plus_2p23(r.x, 1))), cc, w0, w1);
+    edge_weight_pair(f2_sub(b2, f2_pack(byte_plus_2p23(r.x, 2), byte_plus_2p23(r.x, 3))), cc, w2, w3);
+    edge_weight_pair(f2_sub(b2, f2_pack(byte_plus_2p23(r.y, 0), byte_plus_2p23(r.y, 1))), cc, w4, w5);
     mask = r.y >> 16;
   }
   const float c1 = __fadd_rn(w0, w1);

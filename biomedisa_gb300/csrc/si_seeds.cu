@@ -309,11 +309,17 @@ extern "C" int si_extract_seeds_box(const void* labels, int dtype, int Z0, int Y
 // Limit: n_slices * max(Zc, Yc) + 1 <= kStaticRowCounters (1,048,576 counters,
 // 4 MiB, held by every GPU that loads the library until the process exits).
 // The first call on a device looks up the array's device address with that
-// device current; make that first call before any stream capture. All calls
-// share the one array: calls whose work overlaps on the GPU (different streams
-// or threads) race on it. The count pass writes every counter the scan and emit
-// passes read, so nothing left over from an earlier call is ever read.
+// device current; make that first call before any stream capture. The address
+// is remembered together with the device's current CUDA context; when the
+// context changes (after cudaDeviceReset, or when the primary context was
+// released and created again) the module is loaded anew and the next call looks
+// the address up again. All calls share the one array: calls whose work
+// overlaps on the GPU (different streams or threads) race on it. The count pass
+// writes every counter the scan and emit passes read, so nothing left over from
+// an earlier call is ever read.
 // ---------------------------------------------------------------------------
+#include <cuda.h>
+
 #include <mutex>
 
 namespace {
@@ -321,25 +327,53 @@ constexpr unsigned long long kStaticRowCounters = 1ull << 20;
 constexpr int kMaxDevices = 64;
 std::mutex g_static_rows_mu;
 uint32_t* g_static_rows_dev[kMaxDevices] = {};
+CUcontext g_static_rows_ctx[kMaxDevices] = {};
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+
+// The driver's cuCtxGetCurrent through the runtime's entry-point query (the
+// library links only the runtime).
+CtxGetCurrentFn ctx_get_current_fn() {
+  static CtxGetCurrentFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrentFn>(p);
+  });
+  return fn;
+}
 }  // namespace
 
 static __device__ __align__(256) uint32_t g_static_row_counts[kStaticRowCounters];
 
-// Device address of g_static_row_counts for the current device (looked up once
-// per device; the host-side name is not a device address).
+// Device address of g_static_row_counts for the current device and context
+// (looked up once per context; the host-side name is not a device address).
 static int static_row_counts(uint32_t** out) {
   int dev = -1;
   const cudaError_t ge = cudaGetDevice(&dev);
   if (ge != cudaSuccess) return set_error(SI_ERR_CUDA, "si_extract_seeds_noalloc: cudaGetDevice: %s",
                                           cudaGetErrorString(ge));
   if (dev < 0 || dev >= kMaxDevices) return set_error(SI_ERR_LIMIT, "si_extract_seeds_noalloc: device %d", dev);
+  const CtxGetCurrentFn get_ctx = ctx_get_current_fn();
+  if (!get_ctx) return set_error(SI_ERR_CUDA, "si_extract_seeds_noalloc: cuCtxGetCurrent unavailable");
+  CUcontext ctx = nullptr;
+  if (get_ctx(&ctx) != CUDA_SUCCESS)
+    return set_error(SI_ERR_CUDA, "si_extract_seeds_noalloc: cannot read the current context");
   std::lock_guard<std::mutex> lock(g_static_rows_mu);
-  if (!g_static_rows_dev[dev]) {
+  if (!ctx || !g_static_rows_dev[dev] || g_static_rows_ctx[dev] != ctx) {
+    // With no context current yet, the lookup itself makes the device's
+    // primary context current; the context is read again after it.
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_static_row_counts);
     if (e != cudaSuccess || !p)
       return set_error(SI_ERR_CUDA, "si_extract_seeds_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    if (!ctx && (get_ctx(&ctx) != CUDA_SUCCESS || !ctx))
+      return set_error(SI_ERR_CUDA, "si_extract_seeds_noalloc: no current context after the lookup");
     g_static_rows_dev[dev] = static_cast<uint32_t*>(p);
+    g_static_rows_ctx[dev] = ctx;
   }
   *out = g_static_rows_dev[dev];
   return SI_OK;

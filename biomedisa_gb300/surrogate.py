@@ -227,7 +227,13 @@ class SurrogateNet:
         return sd
 
     def load_state_dict(self, sd):
-        """Loads a checkpoint; one without moments (weights only) restarts them at zero."""
+        """Loads a checkpoint. One without moments (weights only) restarts the
+        optimiser: zero moments and step count 0, so AdamW's bias correction
+        starts afresh too. A checkpoint with only some of the moments is
+        refused."""
+        have = [m for m in self._MOMENTS if m in sd]
+        if have and len(have) != len(self._MOMENTS):
+            raise ValueError(f"checkpoint holds only some AdamW moments ({', '.join(have)})")
         if len(sd["w"]) != len(self.convs):
             raise ValueError("checkpoint of a different network depth")
         for i, (c, w, b) in enumerate(zip(self.convs, sd["w"], sd["b"])):
@@ -238,7 +244,7 @@ class SurrogateNet:
             c.wb.copy_(c.w.to(BF16))
             for m in self._MOMENTS:
                 getattr(c, m).copy_(sd[m][i].to(self.device) if m in sd else torch.zeros_like(getattr(c, m)))
-        self.step_count = int(sd.get("step", 0))
+        self.step_count = int(sd.get("step", 0)) if have else 0
 
 
 # ---------------------------------------------------------------------------

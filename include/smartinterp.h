@@ -147,8 +147,10 @@ int si_extract_seeds(const void* labels, int dtype, int Z0, int Y0, int X0,
  * that loads the library, held until exit), so n_slices * max(Zc, Yc) + 1 must
  * not exceed 1,048,576 (SI_ERR_LIMIT otherwise). The first call on a device
  * looks up the array's address with that device current; make it before any
- * stream capture. Calls share the array: calls that overlap on the GPU race.
- * Allocates nothing. */
+ * stream capture. The address is remembered per device with the context it
+ * was looked up in, and looked up again when the device's current context
+ * changes (e.g. after cudaDeviceReset). Calls share the array: calls that
+ * overlap on the GPU race. Allocates nothing. */
 int si_extract_seeds_noalloc(const void* labels, int dtype, int Z0, int Y0,
                              int X0, int cz0, int cy0, int cx0, int Zc,
                              int Yc, int Xc, const int16_t* slot_lut,

@@ -62,7 +62,8 @@ def extract() -> Path:
     from ref_import import REFERENCE_ROOT, capture, reference_modules
 
     if not Path(REFERENCE_ROOT).is_dir():
-        raise FileNotFoundError(f"reference tree not found at {REFERENCE_ROOT}")
+        raise FileNotFoundError(
+            f"reference tree not found at {REFERENCE_ROOT}: set BIOMEDISA_REFERENCE_ROOT to the reference checkout")
     REF.mkdir(exist_ok=True)
     parts = ["/* generated by oracle/ref_extract.py from the reference tree; do not commit */\n"]
     with reference_modules():
@@ -92,9 +93,10 @@ def compile_libs() -> tuple[Path, Path]:
 def build(extract_if_possible: bool = True) -> bool:
     """Extracts (when the reference tree is present) and compiles. Returns
     False when neither the tree nor a previously extracted .inc exists."""
-    from ref_import import REFERENCE_ROOT  # noqa: F401  (path constant only)
+    sys.path.insert(0, str(HERE))
+    from ref_import import REFERENCE_ROOT
 
-    if extract_if_possible and Path("/root/reference").is_dir():
+    if extract_if_possible and Path(REFERENCE_ROOT).is_dir():
         extract()
     if not INC.exists():
         return False

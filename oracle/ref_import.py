@@ -13,11 +13,15 @@ Nothing under the reference tree is written (bytecode writing is disabled).
 from __future__ import annotations
 
 import importlib
+import os
 import sys
 import types
 from contextlib import contextmanager
 
-REFERENCE_ROOT = "/root/reference"
+# Where the reference checkout lives. This recipe reads the reference from
+# there; set BIOMEDISA_REFERENCE_ROOT to use another checkout. Every other file
+# takes the location from here.
+REFERENCE_ROOT = os.environ.get("BIOMEDISA_REFERENCE_ROOT", "/root/reference")
 
 RECORDED_SOURCES: list[str] = []
 

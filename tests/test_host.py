@@ -113,8 +113,8 @@ def test_autotune_cache_round_trip(tmp_path, monkeypatch):
 
 def test_surrogate_checkpoint_round_trip(tmp_path):
     """save/load keep weights, biases, AdamW moments and the step count; a
-    weights-only checkpoint loads with zero moments; a different shape is
-    refused. (The network is built on the CPU device here: no kernel runs.)"""
+    weights-only checkpoint loads with zero moments and step count 0; a
+    partial set of moments and a different shape are refused. (The network is built on the CPU device here: no kernel runs.)"""
     import torch
 
     from biomedisa_gb300 import surrogate as SG
@@ -138,6 +138,31 @@ def test_surrogate_checkpoint_round_trip(tmp_path):
     c = SG.SurrogateNet(device="cpu", seed=2)
     c.load_state_dict(sd)
     assert torch.equal(c.convs[3].w, a.convs[3].w) and not c.convs[3].mw.any()
+    assert c.step_count == 0  # weights only: AdamW restarts, bias correction included
+    partial = a.state_dict()
+    del partial["vb"]
+    with pytest.raises(ValueError):
+        SG.SurrogateNet(device="cpu", seed=2).load_state_dict(partial)
     d = SG.SurrogateNet(channels=32, device="cpu")
     with pytest.raises(ValueError):
         d.load_state_dict(a.state_dict())
+
+
+def test_autotune_store_concurrent_threads(tmp_path, monkeypatch):
+    """Threads of one process storing autotune entries at once keep every
+    entry and leave no temporary files behind."""
+    import threading
+
+    from biomedisa_gb300 import autotune as AT
+
+    path = tmp_path / "cache.json"
+    monkeypatch.setenv("SI_AUTOTUNE_CACHE", str(path))
+    threads = [threading.Thread(target=AT._store, args=(f"k{i}", {"sort_edge": 6, "sweep_steps": i}))
+               for i in range(16)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    data = AT._load()
+    assert sorted(data) == sorted(f"k{i}" for i in range(16))
+    assert [p.name for p in tmp_path.iterdir()] == ["cache.json"]
