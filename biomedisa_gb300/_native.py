@@ -42,6 +42,9 @@ _SIGNATURES = {
     "si_pack_neighbours": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_void_p],
     "si_walk": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_void_p, _c_u32, _c_int, _c_int, _c_u64,
                 _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_walk_refstream": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_void_p, _c_u32, _c_int, _c_int,
+                          _c_void_p, _c_void_p, _c_int, _c_void_p],
+    "si_walk_sorted_set_range": [_c_u64],
     "si_walk_bricks_scratch": [_c_int, _c_int, _c_int, _c_u64, _c_int, _c_void_p],
     "si_walk_bricks": [_c_void_p, _c_int, _c_int, _c_int, _c_void_p, _c_void_p, _c_u32, _c_int, _c_int, _c_u64,
                        _c_void_p, _c_int, _c_void_p, _c_u64, _c_void_p, _c_void_p],
@@ -75,8 +78,11 @@ _SIGNATURES = {
     "si_clean": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, ctypes.c_double, _c_int, _c_void_p, _c_u64,
                  _c_void_p],
     "si_fill": [_c_void_p, _c_int, _c_int, _c_int, ctypes.c_double, _c_void_p, _c_int, _c_void_p, _c_u64, _c_void_p],
-    "si_smooth_f32": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
-    "si_smooth": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_smooth_f32": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_smooth": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_smooth_tmp_floats": [_c_int, _c_int, _c_int, _c_void_p],
+    "si_smooth_status": [_c_void_p, _c_void_p],
+    "si_set_wait_limit": [ctypes.c_longlong],
     "si_geo_normalize": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_void_p, _c_void_p],
     "si_geo_masks": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_int, _c_void_p, _c_void_p],
     "si_geo_scan": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, ctypes.c_double, _c_int, _c_int,

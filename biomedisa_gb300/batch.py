@@ -16,7 +16,7 @@ import torch
 from . import _native as nat
 from . import autotune
 from .interpolation import (DEFAULT_RNG_SEED, DeviceJob, _IMG_DTYPES, _LAB_DTYPES, _err, _ptr, _stream,
-                            normalize_host_dtypes, upload)
+                            normalize_host_dtypes, smooth_buffers, smooth_check, smooth_tmp_floats, upload)
 
 
 class SiVolume(ctypes.Structure):
@@ -153,12 +153,12 @@ def smooth_batch(jobs, graph=True):
     live = [j for j in jobs if j is not None and j.smooth]
     if not live:
         return
-    vmax = max(j.cplan.voxels for j in live)
-    tmp0 = torch.empty(vmax, dtype=torch.float32, device="cuda")
-    tmp1 = torch.empty(vmax, dtype=torch.float32, device="cuda")
+    nmax = max(smooth_tmp_floats(j.cplan.Zc, j.cplan.Yc, j.cplan.Xc) for j in live)
+    tmp0, tmp1 = smooth_buffers(1, 1, 1, "cuda", floats=nmax)
     if not graph:
         for j in live:
             j.smooth_launch(tmp0, tmp1)
+        smooth_check()
         return
     g = torch.cuda.CUDAGraph()
     torch.cuda.synchronize()
@@ -166,7 +166,7 @@ def smooth_batch(jobs, graph=True):
         for j in live:
             j.smooth_launch(tmp0, tmp1)
     g.replay()
-    torch.cuda.current_stream().synchronize()
+    smooth_check()
 
 
 def smart_interpolation_batch(volumes, labels, nbrw=10, sorw=4000, smooth=0, allaxis=False, uncertainty=False,

@@ -26,6 +26,7 @@
 
 #include "si_common.cuh"
 #include "si_internal.h"
+#include "si_tma.cuh"
 
 namespace si {
 namespace {
@@ -37,7 +38,6 @@ constexpr int kExtVox = kExt * kExt * kExt;
 constexpr int kAdvThreads = 512;
 constexpr uint32_t kChunk = 4096;  // sorted walkers per work ticket
 constexpr int kScanBlock = 1024;   // elements per scan block (256 threads x 4)
-constexpr uint32_t kWaitLimit = 1u << 26;
 
 struct BrickGeom {
   int Zc, Yc, Xc;
@@ -219,36 +219,6 @@ __global__ void __launch_bounds__(256) pack_pitched_kernel(const uint8_t* __rest
   }
 }
 
-// ---- TMA / mbarrier helpers (inline PTX) ----
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ void tma_load_box(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(smem_u32(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-      : "memory");
-}
-
 __device__ __forceinline__ float byte_p23(uint32_t w, uint32_t k) {
   return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + k));
 }
@@ -261,7 +231,7 @@ __device__ __forceinline__ uint32_t pick(const U4& r, uint32_t sub) {
 __global__ void __launch_bounds__(kAdvThreads, 4) brick_advance_kernel(
     const __grid_constant__ CUtensorMap rec_map, BrickGeom g, uint4* __restrict__ states,
     const uint32_t* __restrict__ offsets, uint32_t nbt, uint32_t n_live, uint32_t* __restrict__ chunk_ctr, const SeedRec* __restrict__ seeds, uint32_t k0, uint32_t k1,
-    uint32_t* __restrict__ hits, uint32_t* __restrict__ err) {
+    uint32_t* __restrict__ hits, uint32_t* __restrict__ err, uint32_t wait_lim) {
   extern __shared__ __align__(128) uint8_t smem[];
   uint2* s_rec = reinterpret_cast<uint2*>(smem);
   uint32_t* s_hits = reinterpret_cast<uint32_t*>(smem + kExtVox * sizeof(uint2));
@@ -307,18 +277,17 @@ __global__ void __launch_bounds__(kAdvThreads, 4) brick_advance_kernel(
         tma_load_box(s_rec, &rec_map, ex0, ey0, ez0, &s_bar);
       }
       for (int i = tid; i < kExtVox; i += kAdvThreads) s_hits[i] = 0u;
-      bool done = false;
-      for (uint32_t it = 0; it < kWaitLimit; ++it) {
-        if (mbar_try_wait(&s_bar, phase)) {
-          done = true;
-          break;
-        }
-      }
-      phase ^= 1u;
+      const bool done = mbar_wait_bounded(&s_bar, phase, wait_lim);
       if (__syncthreads_or(!done)) {
-        if (tid == 0) atomicOr(err, 1u);
+        // gave up: wait (bounded) for the box copy still in flight before the
+        // CTA's shared memory goes away, then report
+        if (tid == 0) {
+          mbar_wait_bounded(&s_bar, phase, kDrainWaitLimit);
+          atomicOr(err, 1u);
+        }
         return;
       }
+      phase ^= 1u;
       uint32_t* __restrict__ hl = hits + (size_t)slot * V;
       for (;;) {
         const uint32_t w = atomicAdd(&s_next, 1u);
@@ -403,11 +372,14 @@ __global__ void __launch_bounds__(kAdvThreads, 4) brick_advance_kernel(
 // resident at any moment work on a compact slab of the volume and its records
 // and hit counters stay in L2.
 // ---------------------------------------------------------------------------
+// Walkers still live after their K steps are counted into next_counts by
+// (label slot, brick): the counting pass of the next sort, fused (warp
+// aggregation of equal keys; walkers of a warp come from few buckets).
 template <bool kFloat>
 __global__ void __launch_bounds__(256) sweep_kernel(const void* __restrict__ packed, BrickGeom g,
                                                     uint4* __restrict__ states, uint32_t n_live, uint32_t K,
                                                     const SeedRec* __restrict__ seeds, uint32_t k0, uint32_t k1,
-                                                    uint32_t* __restrict__ hits) {
+                                                    uint32_t* __restrict__ hits, uint32_t* __restrict__ next_counts) {
   __shared__ int32_t s_delta[6];
   if (threadIdx.x < 6) {
     const int32_t F = (int32_t)g.F, X = g.Xc;
@@ -417,38 +389,34 @@ __global__ void __launch_bounds__(256) sweep_kernel(const void* __restrict__ pac
   __syncthreads();
   const size_t V = (size_t)g.F * g.Zc;
   const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_live; i += stride) {
-    uint4 st = states[i];
-    const SeedRec sd = seeds[st.y];
-    const uint32_t te = st.w & 0xFFFFFFu;
-    const uint32_t t_end = min(st.z + K, te);
-    uint32_t* __restrict__ hl = hits + (size_t)(st.w >> 24) * V;
-    st.x = walk_steps<kFloat>(packed, st.x, st.z, t_end, sd.c, sd.b, sd.pos, seed_axis(sd.meta),
-                              seed_label(sd.meta), k0, k1, hl, s_delta);
-    st.z = t_end;
-    states[i] = st;
+  const int lane = threadIdx.x & 31;
+  // warp-uniform trip count, so the counting below runs with full warps
+  const uint32_t i_end = (n_live + 31u) & ~31u;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < i_end; i += stride) {
+    bool alive = false;
+    uint4 st = make_uint4(0u, 0u, 0u, 0u);
+    if (i < n_live) {
+      st = states[i];
+      const SeedRec sd = seeds[st.y];
+      const uint32_t te = st.w & 0xFFFFFFu;
+      const uint32_t t_end = min(st.z + K, te);
+      uint32_t* __restrict__ hl = hits + (size_t)(st.w >> 24) * V;
+      st.x = walk_steps<kFloat>(packed, st.x, st.z, t_end, sd.c, sd.b, sd.pos, seed_axis(sd.meta),
+                                seed_label(sd.meta), k0, k1, hl, s_delta);
+      st.z = t_end;
+      states[i] = st;
+      alive = t_end != te;
+    }
+    const uint32_t act = __ballot_sync(0xffffffffu, alive);
+    if (alive) {
+      const uint32_t key = bucket_of(g, st);
+      const uint32_t peers = __match_any_sync(act, key);
+      if (lane == __ffs(peers) - 1) atomicAdd(&next_counts[key], (uint32_t)__popc(peers));
+    }
   }
 }
 
 // ---- host side ----
-using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-  });
-  return fn;
-}
-
 struct ScratchLayout {
   size_t rec, states0, states1, counts, offsets, sums, ctrs, total;
 };
@@ -615,7 +583,7 @@ extern "C" int si_walk_bricks(const void* work, int Zc, int Yc, int Xc, const si
     if (cudaMemsetAsync(ctrs + 1, 0, sizeof(uint32_t), st) != cudaSuccess)
       return set_error(SI_ERR_CUDA, "si_walk_bricks: memset failed");
     brick_advance_kernel<<<adv_grid, kAdvThreads, smem, st>>>(map, g, states[cur], offsets, nbt, live_now, ctrs + 1,
-                                                               sd, k0, k1, hits, ctrs + 2);
+                                                               sd, k0, k1, hits, ctrs + 2, wait_limit());
     const int rc = check_launch("si_walk_bricks: advance");
     if (rc) return rc;
     n_prev = live_now;
@@ -632,11 +600,17 @@ extern "C" int si_walk_bricks(const void* work, int Zc, int Yc, int Xc, const si
 
 namespace si {
 namespace {
-constexpr uint64_t kBatchWalks = 1ull << 25;  // walks per seed range of si_walk_sorted
+constexpr uint64_t kBatchWalks = 1ull << 25;  // default walks per seed range of si_walk_sorted
 constexpr int kSortEdge = 6;
+std::atomic<unsigned long long> g_range_walks{0};  // 0 = kBatchWalks (si_walk_sorted_set_range)
+
+uint64_t range_walks() {
+  const unsigned long long v = g_range_walks.load(std::memory_order_relaxed);
+  return v ? (uint64_t)v : kBatchWalks;
+}
 
 struct SortLayout {
-  size_t states0, states1, counts, offsets, sums, ctrs, total;
+  size_t states0, states1, counts, counts2, offsets, sums, ctrs, total;
 };
 
 SortLayout sort_layout(const BrickGeom& g, uint64_t max_walks, int nol) {
@@ -649,6 +623,8 @@ SortLayout sort_layout(const BrickGeom& g, uint64_t max_walks, int nol) {
   L.states1 = off;
   off = align_up(off + max_walks * sizeof(uint4), 256);
   L.counts = off;
+  off = align_up(off + (nbt + 1) * sizeof(uint32_t), 256);
+  L.counts2 = off;
   off = align_up(off + (nbt + 1) * sizeof(uint32_t), 256);
   L.offsets = off;
   off = align_up(off + (nbt + 1) * sizeof(uint32_t), 256);
@@ -668,6 +644,12 @@ extern "C" int si_walk_sorted_scratch(int Zc, int Yc, int Xc, uint64_t max_walks
   if (!bytes || Zc < 3 || Yc < 3 || Xc < 3 || nol < 1 || nol > 256 || sort_edge < 0 || sort_edge > 1024)
     return set_error(SI_ERR_ARG, "si_walk_sorted_scratch: bad arguments");
   *bytes = sort_layout(make_geom(Zc, Yc, Xc, sort_edge > 0 ? sort_edge : kSortEdge), max_walks, nol).total;
+  return SI_OK;
+}
+
+extern "C" int si_walk_sorted_set_range(unsigned long long walks_per_range) {
+  clear_error();
+  g_range_walks.store(walks_per_range, std::memory_order_relaxed);
   return SI_OK;
 }
 
@@ -702,7 +684,8 @@ extern "C" int si_walk_sorted(const void* packed, int work_is_float, int Zc, int
                      (unsigned long long)L.total);
   uint8_t* base = static_cast<uint8_t*>(scratch);
   uint4* states[2] = {reinterpret_cast<uint4*>(base + L.states0), reinterpret_cast<uint4*>(base + L.states1)};
-  uint32_t* counts = reinterpret_cast<uint32_t*>(base + L.counts);
+  uint32_t* counts = reinterpret_cast<uint32_t*>(base + L.counts);     // this round's bucket sizes
+  uint32_t* counts2 = reinterpret_cast<uint32_t*>(base + L.counts2);   // the next round's, counted by the sweep
   uint32_t* offsets = reinterpret_cast<uint32_t*>(base + L.offsets);
   uint32_t* sums = reinterpret_cast<uint32_t*>(base + L.sums);
   uint32_t* ctrs = reinterpret_cast<uint32_t*>(base + L.ctrs);
@@ -712,61 +695,64 @@ extern "C" int si_walk_sorted(const void* packed, int work_is_float, int Zc, int
   const int sms = sm_count();
   const int gb = sms * 8;
   const uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
-  // Seeds are walked in consecutive ranges of about kBatchWalks walks, each to
-  // completion. Seeds come in slice order, so a range is a compact slab and a
-  // sweep's records and hit counters stay closer to L2 than when every seed of
-  // the volume is live at once (measured: +6 % on a 400x512x512 volume, +19 % on
-  // 1024^3). Hits are integer sums of independent walks: the result does not
-  // depend on the ranges.
-  const uint64_t nbatch = std::max<uint64_t>(1, (walks + kBatchWalks / 2) / kBatchWalks);
+  const size_t count_bytes = (size_t)(nbt + 1) * sizeof(uint32_t);
+  // Seeds are walked in consecutive ranges of about range_walks() walks, each
+  // to completion. Seeds come in slice order, so a range is a compact slab and
+  // a sweep's records and hit counters stay closer to L2 than when every seed
+  // of the volume is live at once (measured: +6 % on a 400x512x512 volume,
+  // +19 % on 1024^3). Hits are integer sums of independent walks: the result
+  // does not depend on the ranges.
+  const uint64_t per_range = range_walks();
+  const uint64_t nbatch = std::max<uint64_t>(1, (walks + per_range / 2) / per_range);
   int rounds = 0;
   for (uint64_t bidx = 0; bidx < nbatch; ++bidx) {
-  const uint32_t sa = (uint32_t)((uint64_t)ns * bidx / nbatch), se = (uint32_t)((uint64_t)ns * (bidx + 1) / nbatch);
-  if (se == sa) continue;
-  const SeedRec* sd = sd_all + sa;
-  const uint32_t ns_b = se - sa;
-  int cur = 0;
-  uint64_t n_prev = (uint64_t)ns_b * (uint64_t)nbrw;
-  for (int batch_rounds = 0;; ++batch_rounds, ++rounds) {
-    const bool first = batch_rounds == 0;
-    if (cudaMemsetAsync(counts, 0, (size_t)(nbt + 1) * sizeof(uint32_t), st) != cudaSuccess)
+    const uint32_t sa = (uint32_t)((uint64_t)ns * bidx / nbatch), se = (uint32_t)((uint64_t)ns * (bidx + 1) / nbatch);
+    if (se == sa) continue;
+    const SeedRec* sd = sd_all + sa;
+    const uint32_t ns_b = se - sa;
+    int cur = 0;
+    uint64_t n_prev = (uint64_t)ns_b * (uint64_t)nbrw;
+    // round 0's bucket sizes come from a counting pass over the virtual
+    // (seed, walk) pairs; every later round's from the previous sweep
+    if (cudaMemsetAsync(counts, 0, count_bytes, st) != cudaSuccess)
       return set_error(SI_ERR_CUDA, "si_walk_sorted: memset failed");
-    if (first)
-      bucket_kernel<true, false><<<gb, 256, 0, st>>>(nullptr, n_prev, sd, ns_b, sorw, g, counts, nullptr, nullptr);
-    else
-      bucket_kernel<false, false><<<gb, 256, 0, st>>>(states[cur], n_prev, sd, ns_b, sorw, g, counts, nullptr,
-                                                      nullptr);
-    scan_sums_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums);
-    scan_top_kernel<<<1, 1024, 0, st>>>(sums, nblocks);
-    scan_apply_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums, offsets, ctrs);
-    uint32_t live_now = 0;
-    if (cudaMemcpyAsync(&live_now, ctrs, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return set_error(SI_ERR_CUDA, "si_walk_sorted: round %d: %s", rounds, cudaGetErrorString(cudaGetLastError()));
-    if (live_now == 0) break;
-    if (cudaMemsetAsync(counts, 0, (size_t)(nbt + 1) * sizeof(uint32_t), st) != cudaSuccess)
-      return set_error(SI_ERR_CUDA, "si_walk_sorted: memset failed");
-    const int nxt = first ? 0 : 1 - cur;
-    if (first)
-      bucket_kernel<true, true><<<gb, 256, 0, st>>>(nullptr, n_prev, sd, ns_b, sorw, g, counts, offsets,
-                                                    states[nxt]);
-    else
-      bucket_kernel<false, true><<<gb, 256, 0, st>>>(states[cur], n_prev, sd, ns_b, sorw, g, counts, offsets,
-                                                     states[nxt]);
-    cur = nxt;
-    const uint64_t want_blocks = ((uint64_t)live_now + 255) / 256;
-    const uint32_t blocks = (uint32_t)(want_blocks < (uint64_t)sms * 8 ? want_blocks : (uint64_t)sms * 8);
-    if (work_is_float)
-      sweep_kernel<true><<<blocks, 256, 0, st>>>(packed, g, states[cur], live_now, (uint32_t)sweep_steps, sd, k0, k1,
-                                                 hits);
-    else
-      sweep_kernel<false><<<blocks, 256, 0, st>>>(packed, g, states[cur], live_now, (uint32_t)sweep_steps, sd, k0,
-                                                  k1, hits);
-    const int rc = check_launch("si_walk_sorted: sweep");
-    if (rc) return rc;
-    n_prev = live_now;
-    if (batch_rounds > (1 << 24)) return set_error(SI_ERR_LIMIT, "si_walk_sorted: no convergence");
-  }
+    bucket_kernel<true, false><<<gb, 256, 0, st>>>(nullptr, n_prev, sd, ns_b, sorw, g, counts, nullptr, nullptr);
+    for (int batch_rounds = 0;; ++batch_rounds, ++rounds) {
+      const bool first = batch_rounds == 0;
+      scan_sums_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums);
+      scan_top_kernel<<<1, 1024, 0, st>>>(sums, nblocks);
+      scan_apply_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums, offsets, ctrs);
+      uint32_t live_now = 0;
+      if (cudaMemcpyAsync(&live_now, ctrs, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        return set_error(SI_ERR_CUDA, "si_walk_sorted: round %d: %s", rounds, cudaGetErrorString(cudaGetLastError()));
+      if (live_now == 0) break;
+      // counts becomes the scatter's per-bucket cursor, counts2 the next round's sizes
+      if (cudaMemsetAsync(counts, 0, count_bytes, st) != cudaSuccess ||
+          cudaMemsetAsync(counts2, 0, count_bytes, st) != cudaSuccess)
+        return set_error(SI_ERR_CUDA, "si_walk_sorted: memset failed");
+      const int nxt = first ? 0 : 1 - cur;
+      if (first)
+        bucket_kernel<true, true><<<gb, 256, 0, st>>>(nullptr, n_prev, sd, ns_b, sorw, g, counts, offsets,
+                                                      states[nxt]);
+      else
+        bucket_kernel<false, true><<<gb, 256, 0, st>>>(states[cur], n_prev, sd, ns_b, sorw, g, counts, offsets,
+                                                       states[nxt]);
+      cur = nxt;
+      const uint64_t want_blocks = ((uint64_t)live_now + 255) / 256;
+      const uint32_t blocks = (uint32_t)(want_blocks < (uint64_t)sms * 8 ? want_blocks : (uint64_t)sms * 8);
+      if (work_is_float)
+        sweep_kernel<true><<<blocks, 256, 0, st>>>(packed, g, states[cur], live_now, (uint32_t)sweep_steps, sd, k0,
+                                                   k1, hits, counts2);
+      else
+        sweep_kernel<false><<<blocks, 256, 0, st>>>(packed, g, states[cur], live_now, (uint32_t)sweep_steps, sd, k0,
+                                                    k1, hits, counts2);
+      const int rc = check_launch("si_walk_sorted: sweep");
+      if (rc) return rc;
+      std::swap(counts, counts2);
+      n_prev = live_now;
+      if (batch_rounds > (1 << 24)) return set_error(SI_ERR_LIMIT, "si_walk_sorted: no convergence");
+    }
   }
   if (rounds_out) *rounds_out = rounds;
   return check_launch("si_walk_sorted");

@@ -2,9 +2,11 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <mutex>
 #include <string>
 
 #include "si_internal.h"
+#include "si_tma.cuh"
 
 namespace si {
 
@@ -44,7 +46,36 @@ int sm_count() {
   return n;
 }
 
+namespace {
+std::atomic<long long> g_wait_limit{-1};  // < 0: kDefaultWaitLimit
+}
+
+uint32_t wait_limit() {
+  const long long v = g_wait_limit.load(std::memory_order_relaxed);
+  return v < 0 ? kDefaultWaitLimit : (uint32_t)(v > 0xFFFFFFFFll ? 0xFFFFFFFFll : v);
+}
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
 }  // namespace si
+
+extern "C" int si_set_wait_limit(long long spins) {
+  si::clear_error();
+  si::g_wait_limit.store(spins, std::memory_order_relaxed);
+  return SI_OK;
+}
 
 extern "C" int si_version(void) { return 100; }
 

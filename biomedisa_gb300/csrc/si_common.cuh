@@ -48,6 +48,43 @@ __device__ __forceinline__ float u01_from_bits(uint32_t bits) {
 }
 
 // ---------------------------------------------------------------------------
+// The reference walker's own random stream (pycuda_small.py:155-165 state
+// set-up, :197-225 update): the recurrence of MRG32k3a written in binary32
+// (its products exceed 2^24, so it is not the integer generator), every
+// operation rounded on its own as the source reads without contraction:
+//   p1 = a12*s11 - a13n*s10; k1 = (long)(p1/m1); p1 -= (float)k1*m1;
+//   p1 < 0 -> p1 += m1; shift; the same for p2 with (a21, a23n, m2);
+//   u = (p1 <= p2 ? (p1 - p2) + m1 : p1 - p2) * norm.
+// All six state words start at the seed's index in the reference's slice
+// stack; the stream runs on across the seed's walks.
+// ---------------------------------------------------------------------------
+struct RefStream {
+  float s10, s11, s12, s20, s21, s22;
+};
+
+__device__ __forceinline__ float ref_stream_next(RefStream& r) {
+  const float m1 = 4294967087.0f, m2 = 4294944443.0f;
+  const float a12 = 1403580.0f, a13n = 810728.0f, a21 = 527612.0f, a23n = 1370589.0f;
+  const float norm = 2.328306549295728e-10f;
+  float p1 = __fsub_rn(__fmul_rn(a12, r.s11), __fmul_rn(a13n, r.s10));
+  long long k1 = __float2ll_rz(__fdiv_rn(p1, m1));
+  p1 = __fsub_rn(p1, __fmul_rn(__ll2float_rn(k1), m1));
+  if (p1 < 0.0f) p1 = __fadd_rn(p1, m1);
+  r.s10 = r.s11;
+  r.s11 = r.s12;
+  r.s12 = p1;
+  float p2 = __fsub_rn(__fmul_rn(a21, r.s22), __fmul_rn(a23n, r.s20));
+  k1 = __float2ll_rz(__fdiv_rn(p2, m2));
+  p2 = __fsub_rn(p2, __fmul_rn(__ll2float_rn(k1), m2));
+  if (p2 < 0.0f) p2 = __fadd_rn(p2, m2);
+  r.s20 = r.s21;
+  r.s21 = r.s22;
+  r.s22 = p2;
+  if (p1 <= p2) return __fmul_rn(__fadd_rn(__fsub_rn(p1, p2), m1), norm);
+  return __fmul_rn(__fsub_rn(p1, p2), norm);
+}
+
+// ---------------------------------------------------------------------------
 // Edge weight w = 2^(-d2 * c), with c = log2(e) / (2 var) per seed, i.e. the
 // Gaussian intensity weight exp(-(B-I)^2 / (2 var)) of the reference walker
 // (biomedisa/features/random_walk/pycuda_small.py:133-136), evaluated by our own
@@ -183,10 +220,11 @@ __device__ __forceinline__ float byte_plus_2p23(uint32_t w, uint32_t k) {
   return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + k));
 }
 
+// One step with the uniform variate u in [0, 1) given.
 template <bool kFloat>
-__device__ __forceinline__ uint32_t walk_step(const void* __restrict__ packed_v, uint32_t pos, uint32_t bits, float c,
-                                              float bf, float b23, uint32_t* __restrict__ hl,
-                                              const int32_t* s_delta) {
+__device__ __forceinline__ uint32_t walk_step_u(const void* __restrict__ packed_v, uint32_t pos, float u, float c,
+                                                float bf, float b23, uint32_t* __restrict__ hl,
+                                                const int32_t* s_delta) {
   float w0, w1, w2, w3, w4, w5;
   uint32_t mask;
   // The (B - I) differences are formed pairwise (+z,-z), (+y,-y), (+x,-x) and
@@ -214,7 +252,7 @@ __device__ __forceinline__ uint32_t walk_step(const void* __restrict__ packed_v,
   const float c3 = __fadd_rn(c2, w3);
   const float c4 = __fadd_rn(c3, w4);
   const float c5 = __fadd_rn(c4, w5);
-  const float rnd = __fmul_rn(c5, u01_from_bits(bits));
+  const float rnd = __fmul_rn(c5, u);
   int dir = (int)(w0 <= rnd) + (int)(c1 <= rnd) + (int)(c2 <= rnd) + (int)(c3 <= rnd) + (int)(c4 <= rnd);
   if (rnd == 0.0f) dir = 0;
   if (!((mask >> dir) & 1u)) {
@@ -222,6 +260,14 @@ __device__ __forceinline__ uint32_t walk_step(const void* __restrict__ packed_v,
     atomicAdd(&hl[pos], 1u);
   }
   return pos;
+}
+
+// One step with u taken from the top 24 bits of a Philox word.
+template <bool kFloat>
+__device__ __forceinline__ uint32_t walk_step(const void* __restrict__ packed_v, uint32_t pos, uint32_t bits, float c,
+                                              float bf, float b23, uint32_t* __restrict__ hl,
+                                              const int32_t* s_delta) {
+  return walk_step_u<kFloat>(packed_v, pos, u01_from_bits(bits), c, bf, b23, hl, s_delta);
 }
 
 __device__ __forceinline__ uint32_t philox_word(const U4& r, uint32_t sub) {

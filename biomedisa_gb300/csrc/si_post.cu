@@ -1,7 +1,11 @@
 // Post-walk kernels: per-voxel argmax (+ optional uncertainty), label remap
 // and curvature smoothing.
+#include <algorithm>
+#include <cstring>
+
 #include "si_common.cuh"
 #include "si_internal.h"
+#include "si_tma.cuh"
 
 namespace si {
 namespace {
@@ -135,126 +139,223 @@ __global__ void __launch_bounds__(256) remap_kernel(uint8_t* __restrict__ out, P
 // Curvature smoothing step (gpu_kernels.py:118-183): on interior voxels
 //   dst = phi + 0.01 * kappa(phi), kappa the level-set mean-curvature term
 // with central differences (sign convention x-1 minus x+1 as in the
-// reference); border voxels copy phi. Every operation is a binary32
-// round-to-nearest operation in the order of the reference expression;
-// /2.0 and /4.0 are exact scalings.
+// reference); border voxels copy phi. kappa is evaluated with binary32
+// round-to-nearest operations in the order of the reference expression
+// (/2.0 and /4.0 are exact scalings). The update is either binary32
+// (phi + RN(0.01f * kappa), the default) or the reference's own arithmetic:
+// `phi += 0.01 * curvature` multiplies by the binary64 literal 0.01 and adds
+// in binary64 before the store rounds to binary32 (gpu_kernels.py:133).
+//
+// Layout: the source of every step is a pitched float32 volume (row pitch
+// Xp = Xc rounded up to 4, so that rows start on 16 bytes), read by TMA
+// tensor copies; the destination may have any row pitch.
+//
+// Schedule: a CTA of 256 threads owns a 64 x 8 column of voxels and marches
+// through kSZ planes in z. Planes arrive in a ring of four shared-memory slots
+// by TMA (one 72 x 10 box per plane: x from x0 - 4 so the copy starts on 16
+// bytes, y from y0 - 1; out-of-volume parts read as zero), issued by one
+// thread two planes ahead of use and completed on per-slot mbarriers. Each
+// thread computes voxels x0 + tx and x0 + 32 + tx of its row as one pair on
+// the packed binary32 pipe (add/sub/mul.rn.f32x2: per lane the same IEEE
+// operation as the scalar form). Of the 19 stencil values a voxel needs, the
+// 10 of planes z-1 and z are carried in registers from the previous plane, so
+// a plane step loads 9 values per voxel from shared memory.
+//
+// Support box: values outside the box of non-(+0) source values grown by
+// one voxel per iteration are exactly +0 (all differences +0, kappa =
+// +0 / (0 + 1e-10) = +0, phi + 0.01 * 0 = +0), so CTAs whose column lies
+// outside it do nothing (or write zeros, when their destination may hold
+// older values).
 // ---------------------------------------------------------------------------
-template <bool kSrcU32>
-__device__ __forceinline__ float ld(const void* p, size_t i) {
-  if (kSrcU32) return __uint2float_rn(static_cast<const uint32_t*>(p)[i]);
-  return static_cast<const float*>(p)[i];
+constexpr int kSX = 64, kSY = 8, kSZ = 32;
+constexpr int kBoxX = kSX + 8, kBoxY = kSY + 2;
+constexpr int kPlaneFloats = kBoxX * kBoxY;  // 720 floats = 2880 bytes per plane
+constexpr int kSlotFloats = 736;             // 2944 bytes: slots 128-byte aligned
+constexpr int kSlots = 4;
+constexpr int kHeadFloats = 64;              // before the pitched volume in tmp1: the support box
+
+// Sticky status of the smoothing kernels (bit 0: a TMA wait gave up); read
+// and cleared by si_smooth_status.
+__device__ uint32_t g_smooth_status;
+
+inline int pitch4(int x) { return (x + 3) & ~3; }
+
+// Support box of one map: b[0..2] = 0x7FFFFFFF - min(z, y, x), b[3..5] =
+// max(z, y, x) + 1, all 0 when the map is all +0 (so one memset empties it).
+__device__ __forceinline__ bool box_outside(const int* __restrict__ b, int grow, int z0, int z1, int y0, int y1,
+                                            int x0, int x1) {
+  if (b[3] == 0) return true;
+  const int bz0 = 0x7FFFFFFF - b[0] - grow, by0 = 0x7FFFFFFF - b[1] - grow, bx0 = 0x7FFFFFFF - b[2] - grow;
+  const int bz1 = b[3] - 1 + grow, by1 = b[4] - 1 + grow, bx1 = b[5] - 1 + grow;
+  return z1 < bz0 || z0 > bz1 || y1 < by0 || y0 > by1 || x1 < bx0 || x0 > bx1;
 }
 
-// 2.5-D tiled smoothing step: a 32x8 tile of threads marches
-// along z over a chunk of planes, keeping planes z-1, z, z+1 of the tile plus a
-// one-voxel halo in shared memory, so every value is read from global memory
-// about 1.3 times per iteration instead of being gathered 19 times.
-constexpr int kTX = 32, kTY = 8, kZChunk = 16;
-
+// src map (uint32 hits or float32) -> pitched float32 copy, and the support
+// box of its non-(+0) values. A warp takes one row at a time.
 template <bool kSrcU32>
-__global__ void __launch_bounds__(kTX * kTY) smooth_tile_kernel(const void* __restrict__ src, float* __restrict__ dst,
-                                                               int Zc, int Yc, int Xc) {
-  __shared__ float pl[3][kTY + 2][kTX + 2];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
-  const int zb = blockIdx.z * kZChunk;
-  const int ze = min(zb + kZChunk, Zc);
-  const size_t X = (size_t)Xc, F = (size_t)Yc * Xc;
-  const int x = x0 + tx, y = y0 + ty;
-  const int tid = ty * kTX + tx;
-  // Each thread fills at most two halo-tile entries per plane; their tile and
-  // in-plane offsets are fixed for the whole z-loop (kLoads: ceil(340 / 256)).
-  constexpr int kTile = (kTY + 2) * (kTX + 2), kLoads = (kTile + kTX * kTY - 1) / (kTX * kTY);
-  int tile_idx[kLoads];
-  int64_t plane_off[kLoads];  // -1: outside the plane (or no entry)
-#pragma unroll
-  for (int k = 0; k < kLoads; ++k) {
-    const int i = tid + k * kTX * kTY;
-    tile_idx[k] = i;
-    plane_off[k] = -1;
-    if (i < kTile) {
-      const int ly = i / (kTX + 2), lx = i - ly * (kTX + 2);
-      const int gy = y0 + ly - 1, gx = x0 + lx - 1;
-      if (gy >= 0 && gy < Yc && gx >= 0 && gx < Xc) plane_off[k] = (int64_t)gy * X + gx;
+__global__ void __launch_bounds__(256) smooth_convert_kernel(const void* __restrict__ src, float* __restrict__ dst,
+                                                             int Zc, int Yc, int Xc, int Xp, int* __restrict__ box) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  int zmin = 0x7FFFFFFF, ymin = 0x7FFFFFFF, xmin = 0x7FFFFFFF, zmax = -1, ymax = -1, xmax = -1;
+  const int rows = Zc * Yc;
+  for (int r = warp; r < rows; r += nwarps) {
+    const size_t si = (size_t)r * Xc, di = (size_t)r * Xp;
+    int rxmin = 0x7FFFFFFF, rxmax = -1;
+    for (int x = lane; x < Xc; x += 32) {
+      float v;
+      if (kSrcU32) v = __uint2float_rn(static_cast<const uint32_t*>(src)[si + x]);
+      else v = static_cast<const float*>(src)[si + x];
+      dst[di + x] = v;
+      if (__float_as_uint(v) != 0u) {
+        rxmin = min(rxmin, x);
+        rxmax = max(rxmax, x);
+      }
+    }
+    if (rxmax >= 0) {
+      const int z = r / Yc, y = r - (r / Yc) * Yc;
+      zmin = min(zmin, z); zmax = max(zmax, z);
+      ymin = min(ymin, y); ymax = max(ymax, y);
+      xmin = min(xmin, rxmin); xmax = max(xmax, rxmax);
     }
   }
-  // loads plane z (zero outside the volume; such values are never used) into
-  // slot sidx and returns the OR of the bit patterns this thread stored
-  auto load_plane = [&](int z, int sidx) -> uint32_t {
-    float* dstp = &pl[sidx][0][0];
-    const bool zin = z >= 0 && z < Zc;
-    uint32_t orv = 0u;
-#pragma unroll
-    for (int k = 0; k < kLoads; ++k) {
-      if (tile_idx[k] < kTile) {
-        const float v = (zin && plane_off[k] >= 0) ? ld<kSrcU32>(src, (size_t)z * F + (size_t)plane_off[k]) : 0.0f;
-        dstp[tile_idx[k]] = v;
-        orv |= __float_as_uint(v);
+  zmin = __reduce_min_sync(0xffffffffu, zmin); ymin = __reduce_min_sync(0xffffffffu, ymin);
+  xmin = __reduce_min_sync(0xffffffffu, xmin); zmax = __reduce_max_sync(0xffffffffu, zmax);
+  ymax = __reduce_max_sync(0xffffffffu, ymax); xmax = __reduce_max_sync(0xffffffffu, xmax);
+  if (lane == 0 && zmax >= 0) {
+    atomicMax(&box[0], 0x7FFFFFFF - zmin); atomicMax(&box[1], 0x7FFFFFFF - ymin);
+    atomicMax(&box[2], 0x7FFFFFFF - xmin); atomicMax(&box[3], zmax + 1);
+    atomicMax(&box[4], ymax + 1); atomicMax(&box[5], xmax + 1);
+  }
+}
+
+template <bool kF64>
+__global__ void __launch_bounds__(256, 3) smooth_tma_kernel(const __grid_constant__ CUtensorMap src,
+                                                            float* __restrict__ dst, int dst_pitch, int Zc, int Yc,
+                                                            int Xc, const int* __restrict__ box, int grow,
+                                                            int write_outside, uint32_t wait_lim) {
+  __shared__ __align__(128) float pl[kSlots][kSlotFloats];
+  __shared__ __align__(8) uint64_t bar[kSlots];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int x0 = blockIdx.x * kSX, y0 = blockIdx.y * kSY, zb = blockIdx.z * kSZ;
+  const int ze = min(zb + kSZ, Zc);
+  const int y = y0 + ty, xa = x0 + tx, xb = x0 + 32 + tx;
+  const size_t dF = (size_t)Yc * dst_pitch;
+  if (box_outside(box, grow, zb, ze - 1, y0, min(y0 + kSY, Yc) - 1, x0, min(x0 + kSX, Xc) - 1)) {
+    if (write_outside && y < Yc) {
+      for (int z = zb; z < ze; ++z) {
+        float* row = dst + (size_t)z * dF + (size_t)y * dst_pitch;
+        if (xa < Xc) row[xa] = 0.0f;
+        if (xb < Xc) row[xb] = 0.0f;
       }
     }
-    return orv;
+    return;
+  }
+  const int nq = ze - zb + 2;  // planes zb-1 .. ze; plane zb-1+q sits in slot q & 3
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kSlots; ++s) mbar_init(&bar[s], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  int issued = 0;  // meaningful in thread 0 only
+  if (threadIdx.x == 0) {
+    fence_proxy_async_shared();
+    for (; issued < kSlots && issued < nq; ++issued) {
+      mbar_expect_tx(&bar[issued], kPlaneFloats * (uint32_t)sizeof(float));
+      tma_load_box(pl[issued], &src, x0 - 4, y0 - 1, zb - 1 + issued, &bar[issued]);
+    }
+  }
+  const int ly = ty + 1;
+  const int ia = ly * kBoxX + tx + 4, ib = ia + 32;
+  auto cross = [&](const float* P, uint64_t& cc, uint64_t& xm, uint64_t& xp, uint64_t& ym, uint64_t& yp) {
+    cc = f2_pack(P[ia], P[ib]);
+    xm = f2_pack(P[ia - 1], P[ib - 1]);
+    xp = f2_pack(P[ia + 1], P[ib + 1]);
+    ym = f2_pack(P[ia - kBoxX], P[ib - kBoxX]);
+    yp = f2_pack(P[ia + kBoxX], P[ib + kBoxX]);
   };
-  // A plane flag is set when any value of the tile's (halo) plane is not +0.0.
-  // When the three planes around z are all +0.0, every stencil of the tile
-  // is +0 and stays exactly +0 (all differences 0, num = +0, +0 / (0 + 1e-10)
-  // = +0), so the block writes the centre values and skips the arithmetic;
-  // hit maps are +0 far from their label's region.
-  int nzm = __syncthreads_or(load_plane(zb - 1, 0) != 0u);
-  int nz0 = __syncthreads_or(load_plane(zb, 1) != 0u);
-  int sm = 0, s0 = 1, sp = 2;
-  for (int z = zb; z < ze; ++z) {
-    const int nzp = __syncthreads_or(load_plane(z + 1, sp) != 0u);
-    const bool quiet = !(nzm | nz0 | nzp);
-    const int lx = tx + 1, ly = ty + 1;
-    const bool inside = x < Xc && y < Yc;
-    const bool interior = inside && z > 0 && y > 0 && x > 0 && z < Zc - 1 && y < Yc - 1 && x < Xc - 1;
-    if (inside) {
-      const float c = pl[s0][ly][lx];
-      const size_t i = (size_t)z * F + (size_t)y * X + x;
-      if (quiet || !interior) {
-        dst[i] = c;
+  auto wait_q = [&](int q) { return mbar_wait_bounded(&bar[q & 3], (uint32_t)(q >> 2) & 1u, wait_lim); };
+
+  uint64_t m_c = 0, m_xm = 0, m_xp = 0, m_ym = 0, m_yp = 0;  // plane z-1
+  uint64_t c_c = 0, c_xm = 0, c_xp = 0, c_ym = 0, c_yp = 0;  // plane z
+  bool ok = wait_q(0);
+  ok = ok && wait_q(1);
+  if (ok) {
+    cross(pl[0], m_c, m_xm, m_xp, m_ym, m_yp);
+    cross(pl[1], c_c, c_xm, c_xp, c_ym, c_yp);
+  }
+  const uint64_t two = f2_splat(2.0f), half = f2_splat(0.5f), quarter = f2_splat(0.25f);
+  const uint64_t eps = f2_splat(1e-10f), hundredth = f2_splat(0.01f);
+  const bool row_in = y < Yc, row_interior = y > 0 && y < Yc - 1;
+  const bool a_in = row_in && xa < Xc, b_in = row_in && xb < Xc;
+  const bool a_int = row_interior && xa > 0 && xa < Xc - 1, b_int = row_interior && xb > 0 && xb < Xc - 1;
+  for (int k = 0; k < ze - zb; ++k) {
+    const int z = zb + k;
+    ok = ok && wait_q(k + 2);
+    if (ok) {
+      const float* C = pl[(k + 1) & 3];
+      const uint64_t k_mm = f2_pack(C[ia - kBoxX - 1], C[ib - kBoxX - 1]);
+      const uint64_t k_pp = f2_pack(C[ia + kBoxX + 1], C[ib + kBoxX + 1]);
+      const uint64_t k_mp = f2_pack(C[ia - kBoxX + 1], C[ib - kBoxX + 1]);
+      const uint64_t k_pm = f2_pack(C[ia + kBoxX - 1], C[ib + kBoxX - 1]);
+      uint64_t p_c, p_xm, p_xp, p_ym, p_yp;  // plane z+1
+      cross(pl[(k + 2) & 3], p_c, p_xm, p_xp, p_ym, p_yp);
+      const uint64_t c2 = f2_mul(two, c_c);
+      const uint64_t dx = f2_mul(f2_sub(c_xm, c_xp), half);
+      const uint64_t dxx = f2_add(f2_sub(c_xm, c2), c_xp);
+      const uint64_t dx2 = f2_mul(dx, dx);
+      const uint64_t dy = f2_mul(f2_sub(c_ym, c_yp), half);
+      const uint64_t dyy = f2_add(f2_sub(c_ym, c2), c_yp);
+      const uint64_t dy2 = f2_mul(dy, dy);
+      const uint64_t dz = f2_mul(f2_sub(m_c, p_c), half);
+      const uint64_t dzz = f2_add(f2_sub(m_c, c2), p_c);
+      const uint64_t dz2 = f2_mul(dz, dz);
+      const uint64_t dxy = f2_mul(f2_sub(f2_sub(f2_add(k_mm, k_pp), k_mp), k_pm), quarter);
+      const uint64_t dxz = f2_mul(f2_sub(f2_sub(f2_add(p_xm, m_xp), p_xp), m_xm), quarter);
+      const uint64_t dyz = f2_mul(f2_sub(f2_sub(f2_add(p_ym, m_yp), p_yp), m_ym), quarter);
+      uint64_t num = f2_add(f2_mul(dxx, f2_add(dy2, dz2)), f2_mul(dyy, f2_add(dx2, dz2)));
+      num = f2_add(num, f2_mul(dzz, f2_add(dx2, dy2)));
+      num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dx), dy), dxy));
+      num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dx), dz), dxz));
+      num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dy), dz), dyz));
+      const uint64_t den = f2_add(f2_add(f2_add(dx2, dy2), dz2), eps);
+      float na, nb, da, db, ca, cb;
+      f2_unpack(num, na, nb);
+      f2_unpack(den, da, db);
+      f2_unpack(c_c, ca, cb);
+      const float ka = __fdiv_rn(na, da), kb = __fdiv_rn(nb, db);
+      float oa, ob;
+      if (kF64) {
+        oa = __double2float_rn(__dadd_rn((double)ca, __dmul_rn(0.01, (double)ka)));
+        ob = __double2float_rn(__dadd_rn((double)cb, __dmul_rn(0.01, (double)kb)));
       } else {
-        const float c2 = __fmul_rn(2.0f, c);
-        const float xm = pl[s0][ly][lx - 1], xp = pl[s0][ly][lx + 1];
-        const float ym = pl[s0][ly - 1][lx], yp = pl[s0][ly + 1][lx];
-        const float zm = pl[sm][ly][lx], zp = pl[sp][ly][lx];
-        const float dx = __fmul_rn(__fsub_rn(xm, xp), 0.5f);
-        const float dxx = __fadd_rn(__fsub_rn(xm, c2), xp);
-        const float dx2 = __fmul_rn(dx, dx);
-        const float dy = __fmul_rn(__fsub_rn(ym, yp), 0.5f);
-        const float dyy = __fadd_rn(__fsub_rn(ym, c2), yp);
-        const float dy2 = __fmul_rn(dy, dy);
-        const float dz = __fmul_rn(__fsub_rn(zm, zp), 0.5f);
-        const float dzz = __fadd_rn(__fsub_rn(zm, c2), zp);
-        const float dz2 = __fmul_rn(dz, dz);
-        const float dxy = __fmul_rn(
-            __fsub_rn(__fsub_rn(__fadd_rn(pl[s0][ly - 1][lx - 1], pl[s0][ly + 1][lx + 1]), pl[s0][ly - 1][lx + 1]),
-                      pl[s0][ly + 1][lx - 1]),
-            0.25f);
-        const float dxz = __fmul_rn(
-            __fsub_rn(__fsub_rn(__fadd_rn(pl[sp][ly][lx - 1], pl[sm][ly][lx + 1]), pl[sp][ly][lx + 1]),
-                      pl[sm][ly][lx - 1]),
-            0.25f);
-        const float dyz = __fmul_rn(
-            __fsub_rn(__fsub_rn(__fadd_rn(pl[sp][ly - 1][lx], pl[sm][ly + 1][lx]), pl[sp][ly + 1][lx]),
-                      pl[sm][ly - 1][lx]),
-            0.25f);
-        float num = __fadd_rn(__fmul_rn(dxx, __fadd_rn(dy2, dz2)), __fmul_rn(dyy, __fadd_rn(dx2, dz2)));
-        num = __fadd_rn(num, __fmul_rn(dzz, __fadd_rn(dx2, dy2)));
-        num = __fsub_rn(num, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, dx), dy), dxy));
-        num = __fsub_rn(num, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, dx), dz), dxz));
-        num = __fsub_rn(num, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, dy), dz), dyz));
-        const float den = __fadd_rn(__fadd_rn(__fadd_rn(dx2, dy2), dz2), 1e-10f);
-        dst[i] = __fadd_rn(c, __fmul_rn(0.01f, __fdiv_rn(num, den)));
+        f2_unpack(f2_add(c_c, f2_mul(hundredth, f2_pack(ka, kb))), oa, ob);
       }
+      const bool z_int = z > 0 && z < Zc - 1;
+      float* row = dst + (size_t)z * dF + (size_t)y * dst_pitch;
+      if (a_in) row[xa] = (z_int && a_int) ? oa : ca;
+      if (b_in) row[xb] = (z_int && b_int) ? ob : cb;
+      m_c = c_c; m_xm = c_xm; m_xp = c_xp; m_ym = c_ym; m_yp = c_yp;
+      c_c = p_c; c_xm = p_xm; c_xp = p_xp; c_ym = p_ym; c_yp = p_yp;
     }
-    __syncthreads();
-    const int t = sm;
-    sm = s0;
-    s0 = sp;
-    sp = t;
-    nzm = nz0;
-    nz0 = nzp;
+    if (__syncthreads_or(!ok)) {
+      // a wait gave up: let the copies still in flight land (bounded) before
+      // the CTA's shared memory goes away, then report
+      if (threadIdx.x == 0) {
+        for (int q = issued > kSlots ? issued - kSlots : 0; q < issued; ++q)
+          mbar_wait_bounded(&bar[q & 3], (uint32_t)(q >> 2) & 1u, kDrainWaitLimit);
+        atomicOr(&g_smooth_status, 1u);
+      }
+      return;
+    }
+    // the slot of plane q = k was last read in step k - 1 (or the prologue): refill it
+    if (threadIdx.x == 0 && issued < nq) {
+      fence_proxy_async_shared();
+      mbar_expect_tx(&bar[issued & 3], kPlaneFloats * (uint32_t)sizeof(float));
+      tma_load_box(pl[issued & 3], &src, x0 - 4, y0 - 1, zb - 1 + issued, &bar[issued & 3]);
+      ++issued;
+    }
   }
 }
 
@@ -307,65 +408,127 @@ extern "C" int si_remap_labels(uint8_t* out, int Zc, int Yc, int Xc, int cz0, in
   return check_launch("si_remap_labels");
 }
 
-extern "C" int si_smooth(uint32_t* maps, float* tmp0, float* tmp1, int nol, int Zc, int Yc, int Xc, int iters,
-                         void* stream) {
-  clear_error();
-  if (!maps || !tmp0 || !tmp1) return set_error(SI_ERR_ARG, "si_smooth: null pointer");
-  if (nol < 1 || nol > 256) return set_error(SI_ERR_ARG, "si_smooth: nol must be 1..256");
-  if (Zc < 1 || Yc < 1 || Xc < 1 || iters < 0) return set_error(SI_ERR_ARG, "si_smooth: bad arguments");
+namespace si {
+namespace {
+
+// Tensor map over a pitched float32 volume (Zc, Yc, Xp) with logical extents
+// (Zc, Yc, Xc): reads beyond Xc, Yc, Zc or below 0 return zero.
+int encode_volume_map(CUtensorMap* map, float* base, int Zc, int Yc, int Xc, const char* what) {
+  const EncodeTiledFn enc = encode_fn();
+  if (!enc) return set_error(SI_ERR_CUDA, "%s: cuTensorMapEncodeTiled unavailable", what);
+  std::memset(map, 0, sizeof(*map));
+  const int Xp = pitch4(Xc);
+  const cuuint64_t dims[3] = {(cuuint64_t)Xc, (cuuint64_t)Yc, (cuuint64_t)Zc};
+  const cuuint64_t strides[2] = {(cuuint64_t)Xp * sizeof(float), (cuuint64_t)Xp * Yc * sizeof(float)};
+  const cuuint32_t boxd[3] = {kBoxX, kBoxY, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult cr = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, boxd, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) return set_error(SI_ERR_CUDA, "%s: tensor map encoding failed (%d)", what, (int)cr);
+  return SI_OK;
+}
+
+// Smoothing of nol maps (uint32 hits when kSrcU32, else float32) of
+// Zc*Yc*Xc voxels; results as float32 in place. tmp0 holds the pitched
+// source of odd iterations, tmp1 its 64-float head (the support box) and the
+// pitched source of even iterations.
+template <bool kSrcU32>
+int smooth_maps(void* maps, float* tmp0, float* tmp1, int nol, int Zc, int Yc, int Xc, int iters, int update,
+                cudaStream_t st, const char* what) {
   const size_t V = (size_t)Zc * Yc * Xc;
-  const int block = 256, grid = grid_for(V, block);
-  const dim3 tblock(kTX, kTY);
-  const dim3 tgrid((Xc + kTX - 1) / kTX, (Yc + kTY - 1) / kTY, (Zc + kZChunk - 1) / kZChunk);
-  cudaStream_t st = as_stream(stream);
+  const int Xp = pitch4(Xc);
+  int* box = reinterpret_cast<int*>(tmp1);
+  float* tmp1v = tmp1 + kHeadFloats;
+  if (iters > 0 && ((reinterpret_cast<uintptr_t>(tmp0) | reinterpret_cast<uintptr_t>(tmp1)) & 15u))
+    return set_error(SI_ERR_ARG, "%s: tmp0/tmp1 must be 16-byte aligned", what);
+  CUtensorMap map0, map1;
+  if (iters > 0) {
+    int rc = encode_volume_map(&map0, tmp0, Zc, Yc, Xc, what);
+    if (rc) return rc;
+    rc = encode_volume_map(&map1, tmp1v, Zc, Yc, Xc, what);
+    if (rc) return rc;
+  }
+  const dim3 grid((Xc + kSX - 1) / kSX, (Yc + kSY - 1) / kSY, (Zc + kSZ - 1) / kSZ);
+  const int cgrid = std::max(1, std::min(sm_count() * 8, (Zc * Yc + 7) / 8));
+  const uint32_t wl = wait_limit();
   for (int l = 0; l < nol; ++l) {
-    uint32_t* m = maps + (size_t)l * V;
-    float* mf = reinterpret_cast<float*>(m);
+    void* m = static_cast<uint8_t*>(maps) + (size_t)l * V * 4;
+    float* mf = static_cast<float*>(m);
     if (iters == 0) {
-      u32_to_f32_kernel<<<grid, block, 0, st>>>(m, mf, V);
+      if (kSrcU32) u32_to_f32_kernel<<<grid_for(V, 256), 256, 0, st>>>(static_cast<uint32_t*>(m), mf, V);
       continue;
     }
-    // iteration 1 reads the uint32 hits; later ones ping-pong; the last one
-    // writes into the map itself (its hits were consumed by iteration 1).
-    float* bufs[2] = {tmp0, tmp1};
-    const void* src = m;
+    if (cudaMemsetAsync(box, 0, 6 * sizeof(int), st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "%s: memset failed", what);
+    smooth_convert_kernel<kSrcU32><<<cgrid, 256, 0, st>>>(m, tmp0, Zc, Yc, Xc, Xp, box);
     for (int it = 1; it <= iters; ++it) {
-      float* dst = (it == iters && it > 1) ? mf : bufs[it & 1];
-      if (it == 1)
-        smooth_tile_kernel<true><<<tgrid, tblock, 0, st>>>(src, dst, Zc, Yc, Xc);
+      const bool last = it == iters;
+      const CUtensorMap& sm = (it & 1) ? map0 : map1;
+      float* dst = last ? mf : ((it & 1) ? tmp1v : tmp0);
+      const int pitch = last ? Xc : Xp;
+      // only iteration 1's destination (tmp1) may hold another map's values
+      // outside the support; every later destination is +0 there already
+      const int write_outside = (it == 1 && !last) ? 1 : 0;
+      if (update)
+        smooth_tma_kernel<true><<<grid, 256, 0, st>>>(sm, dst, pitch, Zc, Yc, Xc, box, it, write_outside, wl);
       else
-        smooth_tile_kernel<false><<<tgrid, tblock, 0, st>>>(src, dst, Zc, Yc, Xc);
-      src = dst;
-    }
-    if (iters == 1) {
-      if (cudaMemcpyAsync(mf, src, V * sizeof(float), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
-        return set_error(SI_ERR_CUDA, "si_smooth: copy failed");
+        smooth_tma_kernel<false><<<grid, 256, 0, st>>>(sm, dst, pitch, Zc, Yc, Xc, box, it, write_outside, wl);
     }
   }
-  return check_launch("si_smooth");
+  return check_launch(what);
+}
+
+int smooth_args(const void* maps, const float* tmp0, const float* tmp1, int nol, int Zc, int Yc, int Xc, int iters,
+                int update, const char* what) {
+  if (!maps || !tmp0 || !tmp1) return set_error(SI_ERR_ARG, "%s: null pointer", what);
+  if (nol < 1 || nol > 256) return set_error(SI_ERR_ARG, "%s: nol must be 1..256", what);
+  if (Zc < 1 || Yc < 1 || Xc < 1 || iters < 0) return set_error(SI_ERR_ARG, "%s: bad arguments", what);
+  if (update != SI_SMOOTH_F32 && update != SI_SMOOTH_REF_F64)
+    return set_error(SI_ERR_ARG, "%s: update must be SI_SMOOTH_F32 or SI_SMOOTH_REF_F64", what);
+  if ((unsigned long long)Zc * Yc * pitch4(Xc) >= (1ull << 40))
+    return set_error(SI_ERR_LIMIT, "%s: volume too large", what);
+  return SI_OK;
+}
+
+}  // namespace
+}  // namespace si
+
+extern "C" int si_smooth_tmp_floats(int Zc, int Yc, int Xc, unsigned long long* n) {
+  clear_error();
+  if (!n || Zc < 1 || Yc < 1 || Xc < 1) return set_error(SI_ERR_ARG, "si_smooth_tmp_floats: bad arguments");
+  *n = (unsigned long long)Zc * Yc * pitch4(Xc) + kHeadFloats;
+  return SI_OK;
+}
+
+extern "C" int si_smooth(uint32_t* maps, float* tmp0, float* tmp1, int nol, int Zc, int Yc, int Xc, int iters,
+                         int update, void* stream) {
+  clear_error();
+  const int rc = smooth_args(maps, tmp0, tmp1, nol, Zc, Yc, Xc, iters, update, "si_smooth");
+  if (rc) return rc;
+  return smooth_maps<true>(maps, tmp0, tmp1, nol, Zc, Yc, Xc, iters, update, as_stream(stream), "si_smooth");
 }
 
 extern "C" int si_smooth_f32(float* maps, float* tmp0, float* tmp1, int nol, int Zc, int Yc, int Xc, int iters,
-                             void* stream) {
+                             int update, void* stream) {
   clear_error();
-  if (!maps || !tmp0 || !tmp1) return set_error(SI_ERR_ARG, "si_smooth_f32: null pointer");
-  if (nol < 1 || nol > 256) return set_error(SI_ERR_ARG, "si_smooth_f32: nol must be 1..256");
-  if (Zc < 1 || Yc < 1 || Xc < 1 || iters < 0) return set_error(SI_ERR_ARG, "si_smooth_f32: bad arguments");
-  const size_t V = (size_t)Zc * Yc * Xc;
-  const dim3 tblock(kTX, kTY);
-  const dim3 tgrid((Xc + kTX - 1) / kTX, (Yc + kTY - 1) / kTY, (Zc + kZChunk - 1) / kZChunk);
+  const int rc = smooth_args(maps, tmp0, tmp1, nol, Zc, Yc, Xc, iters, update, "si_smooth_f32");
+  if (rc) return rc;
+  return smooth_maps<false>(maps, tmp0, tmp1, nol, Zc, Yc, Xc, iters, update, as_stream(stream), "si_smooth_f32");
+}
+
+extern "C" int si_smooth_status(int* status, void* stream) {
+  clear_error();
+  if (!status) return set_error(SI_ERR_ARG, "si_smooth_status: null pointer");
   cudaStream_t st = as_stream(stream);
-  for (int l = 0; l < nol && iters > 0; ++l) {
-    float* m = maps + (size_t)l * V;
-    float* bufs[2] = {tmp0, tmp1};
-    const float* src = m;
-    for (int it = 1; it <= iters; ++it) {
-      float* dst = (it == iters && it > 1) ? m : bufs[it & 1];
-      smooth_tile_kernel<false><<<tgrid, tblock, 0, st>>>(src, dst, Zc, Yc, Xc);
-      src = dst;
-    }
-    if (iters == 1 && cudaMemcpyAsync(m, src, V * sizeof(float), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
-      return set_error(SI_ERR_CUDA, "si_smooth_f32: copy failed");
-  }
-  return check_launch("si_smooth_f32");
+  uint32_t v = 0;
+  const uint32_t zero = 0;
+  if (cudaMemcpyFromSymbolAsync(&v, g_smooth_status, sizeof(v), 0, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess ||
+      cudaMemcpyToSymbolAsync(g_smooth_status, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return set_error(SI_ERR_CUDA, "si_smooth_status: %s", cudaGetErrorString(cudaGetLastError()));
+  *status = (int)v;
+  if (v) return set_error(SI_ERR_CUDA, "smoothing: a TMA wait gave up (status %u)", v);
+  return SI_OK;
 }

@@ -109,10 +109,88 @@ __global__ void __launch_bounds__(256) walk_kernel(const void* __restrict__ pack
   }
 }
 
+// ---------------------------------------------------------------------------
+// Walker on the reference's own random stream (ref_stream_next): one thread
+// per seed runs the seed's nbrw walks of sorw steps one after the other, the
+// stream continuing across walks as in the reference kernel
+// (pycuda_small.py:180-254). The stream of a seed starts at its index in the
+// reference's slice stack: rank * R * C + r * C + c, where rank is the
+// seed's slice among the listed slices of its axis (stack_rank) and (r, c) /
+// (R, C) its in-slice position / the slice's size (pycuda_small.py:145-165;
+// the all-axis kernels index their per-axis stacks the same way). Weights,
+// border rule and hits are those of walk_step.
+// ---------------------------------------------------------------------------
+template <bool kFloat>
+__global__ void __launch_bounds__(128) walk_refstream_kernel(const void* __restrict__ packed_v, int Zc, int Yc, int Xc,
+                                                             const SeedRec* __restrict__ seeds,
+                                                             const uint32_t* __restrict__ n_seeds_ptr,
+                                                             uint32_t max_seeds, int nbrw, int sorw,
+                                                             const int32_t* __restrict__ stack_rank,
+                                                             uint32_t* __restrict__ hits) {
+  __shared__ int32_t s_delta[6];
+  const uint32_t F = (uint32_t)Yc * (uint32_t)Xc;
+  if (threadIdx.x < 6) {
+    const int32_t d[6] = {(int32_t)F, -(int32_t)F, Xc, -Xc, 1, -1};
+    s_delta[threadIdx.x] = d[threadIdx.x];
+  }
+  __syncthreads();
+  const uint32_t ns = min(*n_seeds_ptr, max_seeds);
+  const size_t V = (size_t)F * Zc;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += stride) {
+    const SeedRec sd = seeds[s];
+    const uint32_t z = sd.pos / F, rem = sd.pos - z * F;
+    const uint32_t y = rem / (uint32_t)Xc, x = rem - y * (uint32_t)Xc;
+    const uint32_t axis = seed_axis(sd.meta);
+    int32_t index;
+    if (axis == 0)
+      index = stack_rank[z] * (int32_t)F + (int32_t)(y * Xc + x);
+    else if (axis == 1)
+      index = stack_rank[Zc + y] * (Zc * Xc) + (int32_t)(z * Xc + x);
+    else
+      index = stack_rank[Zc + Yc + x] * (Zc * Yc) + (int32_t)(z * Yc + y);
+    const float init = __int2float_rn(index);
+    RefStream r{init, init, init, init, init, init};
+    uint32_t* __restrict__ hl = hits + (size_t)seed_slot(sd.meta) * V;
+    const float b23 = __fadd_rn(sd.b, 8388608.0f);
+    for (int w = 0; w < nbrw; ++w) {
+      uint32_t pos = sd.pos;
+      for (int t = 0; t < sorw; ++t)
+        pos = walk_step_u<kFloat>(packed_v, pos, ref_stream_next(r), sd.c, sd.b, b23, hl, s_delta);
+    }
+  }
+}
+
 }  // namespace
 }  // namespace si
 
 using namespace si;
+
+extern "C" int si_walk_refstream(const void* packed, int work_is_float, int Zc, int Yc, int Xc,
+                                 const si_seed_t* seeds, const uint32_t* n_seeds, uint32_t max_seeds, int nbrw,
+                                 int sorw, const int32_t* stack_rank, uint32_t* hits, int nol, void* stream) {
+  clear_error();
+  if (!packed || !seeds || !n_seeds || !hits || !stack_rank)
+    return set_error(SI_ERR_ARG, "si_walk_refstream: null pointer");
+  if (Zc < 3 || Yc < 3 || Xc < 3) return set_error(SI_ERR_ARG, "si_walk_refstream: bad dims");
+  if ((uint64_t)Zc * Yc * Xc > 0x7FFFFFFFull)
+    return set_error(SI_ERR_LIMIT, "si_walk_refstream: volume above 2^31 voxels (the reference's int indices)");
+  if (nbrw < 0 || sorw < 0) return set_error(SI_ERR_ARG, "si_walk_refstream: negative nbrw/sorw");
+  if (nol < 1 || nol > 256) return set_error(SI_ERR_ARG, "si_walk_refstream: nol must be 1..256");
+  if (nbrw == 0 || sorw == 0 || max_seeds == 0) return SI_OK;
+  const int block = 128;
+  const uint64_t want = ((uint64_t)max_seeds + block - 1) / block, cap = (uint64_t)sm_count() * 16;
+  const int grid = (int)(want < cap ? want : cap);
+  const SeedRec* sd = reinterpret_cast<const SeedRec*>(seeds);
+  cudaStream_t st = as_stream(stream);
+  if (work_is_float)
+    walk_refstream_kernel<true><<<grid, block, 0, st>>>(packed, Zc, Yc, Xc, sd, n_seeds, max_seeds, nbrw, sorw,
+                                                        stack_rank, hits);
+  else
+    walk_refstream_kernel<false><<<grid, block, 0, st>>>(packed, Zc, Yc, Xc, sd, n_seeds, max_seeds, nbrw, sorw,
+                                                         stack_rank, hits);
+  return check_launch("si_walk_refstream");
+}
 
 extern "C" int si_pack_neighbours(const void* work, int work_is_float, int Zc, int Yc, int Xc, void* packed,
                                   void* stream) {

@@ -40,6 +40,12 @@ def _err(message: str):
     return None
 
 
+# update arithmetic of the smoothing step (include/smartinterp.h si_smooth_update)
+SMOOTH_UPDATES = {"f32": 0, "ref_f64": 1}
+# random stream of the walk: the counter-based Philox stream (default) or the
+# reference walker's own binary32 MRG recurrence (si_walk_refstream)
+RNGS = ("philox", "reference")
+
 SMOOTH_OOM_WARNING = "Warning: GPU out of memory to allocate smooth array. Process continues without smoothing."
 UNCERTAINTY_OOM_WARNING = ("Warning: GPU out of memory to allocate uncertainty array. Process continues without "
                            "uncertainty.")
@@ -54,6 +60,27 @@ def _or_warn_on_oom(make, warning: str):
     except torch.cuda.OutOfMemoryError:
         print(warning)
         return None
+
+
+def smooth_tmp_floats(Zc: int, Yc: int, Xc: int) -> int:
+    """Floats each si_smooth scratch buffer holds for a (Zc, Yc, Xc) crop."""
+    n = ctypes.c_ulonglong(0)
+    nat.call("si_smooth_tmp_floats", Zc, Yc, Xc, ctypes.byref(n))
+    return int(n.value)
+
+
+def smooth_buffers(Zc: int, Yc: int, Xc: int, device=None, floats: int = 0):
+    """The two float32 scratch buffers of si_smooth / si_smooth_f32 (at least
+    ``floats`` each)."""
+    n = max(smooth_tmp_floats(Zc, Yc, Xc), int(floats))
+    return (torch.empty(n, dtype=torch.float32, device=device), torch.empty(n, dtype=torch.float32, device=device))
+
+
+def smooth_check():
+    """Raises when a smoothing kernel's bounded wait gave up since the last
+    check (synchronises the current stream)."""
+    st = ctypes.c_int(0)
+    nat.call("si_smooth_status", ctypes.byref(st), _stream())
 
 
 def _stream() -> int:
@@ -229,13 +256,21 @@ class DeviceJob:
     def __init__(self, img: torch.Tensor, img_code: int, lab: torch.Tensor, lab_code: int, *, nbrw=10, sorw=4000,
                  allaxis=False, smooth=0, uncertainty=False, denoise=False, only="all", ignore="none",
                  rng_seed=DEFAULT_RNG_SEED, walk_grid=0, walk_block=0, walk_order=0, walker="auto",
-                 sweep_steps=0, sort_edge=0, seeding="plain"):
+                 sweep_steps=0, sort_edge=0, seeding="plain", rng="philox", smooth_update="f32"):
         if walker not in WALKERS:
             raise ValueError(f"walker must be one of {WALKERS}")
         if seeding not in SEEDINGS:
             raise ValueError(f"seeding must be one of {SEEDINGS}")
         if seeding == "large" and allaxis:
             raise ValueError("large-path seeding is supported for z-slices only (allaxis=False)")
+        if smooth_update not in SMOOTH_UPDATES:
+            raise ValueError(f"smooth_update must be one of {tuple(SMOOTH_UPDATES)}")
+        self.smooth_update = smooth_update
+        if rng not in RNGS:
+            raise ValueError(f"rng must be one of {RNGS}")
+        if rng == "reference" and seeding == "large":
+            raise ValueError("rng='reference' is supported with the plain seed set only")
+        self.rng = rng
         self.seeding = seeding
         self.sweep_steps = int(sweep_steps)
         self.sort_edge = int(sort_edge)
@@ -333,7 +368,9 @@ class DeviceJob:
             self.launches += 3
         long_walks = self.nbrw * self.sorw >= (1 << 24)
         kind = self.walker
-        if kind == "auto":
+        if self.rng == "reference":
+            kind = "refstream"  # one thread per seed over packed records
+        elif kind == "auto":
             kind = "packed" if long_walks else "sorted"
         if kind == "tiles" and (self.work_is_float or long_walks):
             raise ValueError("the tile walker needs a uint8 volume and nbrw*sorw < 2^24")
@@ -374,6 +411,21 @@ class DeviceJob:
             self.rounds = walk_bricks(self.work, cp.Zc, cp.Yc, cp.Xc, self.seeds, self.n_seeds, self.seed_capacity,
                                       self.nbrw, self.sorw, self.rng_seed, self.hits, nol)
             self.launches += 1 + 9 * self.rounds
+            return
+        if self.walker_used == "refstream":
+            # the reference's stream: one thread per seed, its walks in sequence;
+            # rank of every listed slice among the listed slices of its axis
+            rank = np.full(cp.Zc + cp.Yc + cp.Xc, -1, np.int32)
+            base = {0: 0, 1: cp.Zc, 2: cp.Zc + cp.Yc}
+            count = {0: 0, 1: 0, 2: 0}
+            for a, k in cp.slice_list.tolist():
+                rank[base[a] + k] = count[a]
+                count[a] += 1
+            rank_t = torch.from_numpy(rank).to(self.dev)
+            nat.call("si_walk_refstream", _ptr(self.packed), int(self.work_is_float), cp.Zc, cp.Yc, cp.Xc,
+                     _ptr(self.seeds), _ptr(self.n_seeds), self.seed_capacity, self.nbrw, self.sorw, _ptr(rank_t),
+                     _ptr(self.hits), nol, _stream())
+            self.launches += 1
             return
         if self.walker_used == "sorted":
             self.rounds = walk_sorted(self.packed, self.work_is_float, cp.Zc, cp.Yc, cp.Xc, self.seeds,
@@ -423,11 +475,12 @@ class DeviceJob:
 
     def smooth_launch(self, tmp0: torch.Tensor, tmp1: torch.Tensor):
         """Launches the smoothing iterations (in place on the hit maps); only
-        kernel launches on the current stream, so it can be graph-captured."""
+        kernel launches and memsets on the current stream, so it can be
+        graph-captured. tmp0/tmp1: smooth_buffers() of at least this crop."""
         cp = self.cplan
         nat.call("si_smooth", _ptr(self.hits), _ptr(tmp0), _ptr(tmp1), self.lplan.nol, cp.Zc, cp.Yc, cp.Xc,
-                 self.smooth, _stream())
-        self.launches += self.lplan.nol * max(self.smooth, 1)
+                 self.smooth, SMOOTH_UPDATES[self.smooth_update], _stream())
+        self.launches += self.lplan.nol * (self.smooth + 1 if self.smooth else 1)
 
     def post_smooth(self):
         if self.seeding == "large":
@@ -443,13 +496,12 @@ class DeviceJob:
         res = self.post_regular(return_hits)
         if self.smooth:
             cp = self.cplan
-            tmp = _or_warn_on_oom(lambda: (torch.empty(cp.voxels, dtype=torch.float32, device=self.dev),
-                                           torch.empty(cp.voxels, dtype=torch.float32, device=self.dev)),
-                                  SMOOTH_OOM_WARNING)
+            tmp = _or_warn_on_oom(lambda: smooth_buffers(cp.Zc, cp.Yc, cp.Xc, self.dev), SMOOTH_OOM_WARNING)
             if tmp is None:
                 self.smooth = 0
             else:
                 self.smooth_launch(*tmp)
+                smooth_check()
                 res["smooth"] = self.post_smooth()
         return res
 
@@ -561,7 +613,7 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
                         return_hits=False, img_id=None, label_id=None, remote=False, queue=0, clean=None, fill=None,
                         slicer=False, *, rng_seed=DEFAULT_RNG_SEED, device=None, return_device=False,
                         walk_grid=0, walk_block=0, walk_order=0, walker="auto", sweep_steps=0, sort_edge=0,
-                        seeding="plain"):
+                        seeding="plain", rng="philox", smooth_update="f32"):
     """Smart interpolation of sparsely pre-segmented slices on one GB300.
 
     Same parameters and result keys as the reference
@@ -579,6 +631,14 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
     ``walk_order``). All walkers give identical hit maps. ``seeding='large'``
     walks the seed set of the reference's large path (slice skipping, label
     box, adaptive seeds; z-slices only) instead of every seed.
+    ``rng``: the walk's random stream — 'philox' (counter-based Philox4x32-10
+    keyed by ``rng_seed``, the default) or 'reference' (the reference walker's
+    own binary32 MRG recurrence, seeded per seed as its CUDA kernel does,
+    pycuda_small.py:155-225; one thread per seed, slower), which reproduces
+    the reference's own labels up to the last bits of the exp weights.
+    ``smooth_update``: arithmetic of the smoothing update phi + 0.01 * kappa —
+    'f32' (binary32, the default) or 'ref_f64' (the reference's binary64
+    product and sum, gpu_kernels.py:133, rounded to binary32 on the store).
     """
     if data is None or labelData is None:
         raise NotImplementedError("loading volumes from files is outside this package; pass numpy arrays")
@@ -598,7 +658,7 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
                     sorw=sorw, allaxis=allaxis, smooth=smooth, uncertainty=uncertainty, denoise=denoise, only=only,
                     ignore=ignore, rng_seed=rng_seed, walk_grid=walk_grid, walk_block=walk_block,
                     walk_order=walk_order, walker=walker, sweep_steps=sweep_steps, sort_edge=sort_edge,
-                    seeding=seeding)
+                    seeding=seeding, rng=rng, smooth_update=smooth_update)
     msg = job.analyze()
     if msg:
         return _err(msg)

@@ -511,7 +511,7 @@ def seeds_near(job, mask: torch.Tensor, radius: int, coarse: int = 8) -> torch.T
 
 
 def hybrid_interpolation(img, lab, net: SurrogateNet, nbrw=10, sorw=4000, smooth=0, threshold=0.97, radius=16,
-                         coarse=4, grow=2, rng_seed=None, device_inputs=None, keep_maps=False):
+                         coarse=4, grow=2, rng_seed=None, device_inputs=None, keep_maps=False, smooth_update="f32"):
     """Surrogate probabilities everywhere; the plain walk only from the seeds
     within about `radius` voxels of a voxel whose largest probability is below
     `threshold`, grown by `grow` voxels (the uncertain voxels; the seed
@@ -520,6 +520,7 @@ def hybrid_interpolation(img, lab, net: SurrogateNet, nbrw=10, sorw=4000, smooth
     surrogate's probabilities. Labels are the argmax of the combined maps
     (and of their smoothed copy when smooth > 0), remapped like the plain
     method's. Returns (dict of device label volumes, stats)."""
+    from . import interpolation as I
     from .interpolation import (DEFAULT_RNG_SEED, DeviceJob, SEED_RECORD_BYTES, _IMG_DTYPES, _LAB_DTYPES,
                                 normalize_host_dtypes, upload, walk_sorted)
 
@@ -578,9 +579,10 @@ def hybrid_interpolation(img, lab, net: SurrogateNet, nbrw=10, sorw=4000, smooth
     res = {}
     res["regular"], _ = job._labels_from(probs, True, False)
     if smooth:
-        tmp0 = torch.empty(cp.voxels, dtype=torch.float32, device=job.dev)
-        tmp1 = torch.empty(cp.voxels, dtype=torch.float32, device=job.dev)
-        nat.call("si_smooth_f32", _p(probs), _p(tmp0), _p(tmp1), nol, cp.Zc, cp.Yc, cp.Xc, smooth, _stream())
+        tmp0, tmp1 = I.smooth_buffers(cp.Zc, cp.Yc, cp.Xc, job.dev)
+        nat.call("si_smooth_f32", _p(probs), _p(tmp0), _p(tmp1), nol, cp.Zc, cp.Yc, cp.Xc, smooth,
+                 I.SMOOTH_UPDATES[smooth_update], _stream())
+        I.smooth_check()
         res["smooth"], _ = job._labels_from(probs, True, False)
     torch.cuda.synchronize()
     t4 = time.perf_counter()

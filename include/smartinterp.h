@@ -228,6 +228,34 @@ int si_walk_sorted(const void* packed, int work_is_float, int Zc, int Yc,
                    void* scratch, unsigned long long scratch_bytes,
                    int* rounds_out, void* stream);
 
+/* Size of si_walk_sorted's seed ranges. The walker takes the seeds (which
+ * come in slice order, i.e. as compact slabs) in consecutive ranges of about
+ * walks_per_range walks and walks each range to completion; 0 restores the
+ * default of 2^25. Process-wide; the hit maps do not depend on it (integer
+ * sums of independent walks), only the speed does. No counterpart in the
+ * reference (its walker takes all seeds of a label in one launch,
+ * pycuda_small.py:102-108); tests use it to split small volumes into many
+ * ranges. */
+int si_walk_sorted_set_range(unsigned long long walks_per_range);
+
+/* Walker on the reference's own random stream: the same walk as si_walk
+ * (packed records, weights, border rule, one uint32 hit per accepted move)
+ * with u drawn from the reference walker's binary32 "MRG32k3a" recurrence
+ * (pycuda_small.py:155-165 set-up, :197-225 update), each operation rounded
+ * on its own. One thread per seed runs the seed's nbrw walks in sequence, the
+ * stream continuing across walks. A seed's stream starts at its index in the
+ * reference's slice stack, rank * R * C + r * C + c (pycuda_small.py:145,165):
+ * stack_rank[Zc + Yc + Xc] holds, for axis 0 at [0, Zc), axis 1 at
+ * [Zc, Zc + Yc) and axis 2 at [Zc + Yc, Zc + Yc + Xc), the rank of each listed
+ * slice among the listed slices of its axis (-1 when not listed). Replaces
+ * the reference walker kernels with their own randomness (pycuda_small.py:
+ * 138-257, pycuda_small_allx.py:186-330). */
+int si_walk_refstream(const void* packed, int work_is_float, int Zc, int Yc,
+                      int Xc, const si_seed_t* seeds, const uint32_t* n_seeds,
+                      uint32_t max_seeds, int nbrw, int sorw,
+                      const int32_t* stack_rank, uint32_t* hits, int nol,
+                      void* stream);
+
 /* Scratch bytes si_walk_sorted_batch needs for these volumes (host array of
  * n_vols descriptors, at most 256). */
 int si_walk_sorted_batch_scratch(const si_volume_t* vols, int n_vols,
@@ -265,17 +293,48 @@ int si_remap_labels(uint8_t* out, int Zc, int Yc, int Xc, int cz0, int cy0,
                     int cx0, int Z0, int Y0, int X0, const uint32_t* presence,
                     const uint8_t* all_labels, int nol, void* stream);
 
+/* Update arithmetic of the smoothing step phi + 0.01 * kappa. */
+enum si_smooth_update {
+  SI_SMOOTH_F32 = 0,     /* binary32: phi + RN(0.01f * kappa) */
+  SI_SMOOTH_REF_F64 = 1  /* the reference's `phi += 0.01 * curvature`
+                            (gpu_kernels.py:133): binary64 product with the
+                            binary64 literal 0.01, binary64 sum, rounded to
+                            binary32 on the store */
+};
+
+/* Floats each of si_smooth's tmp0/tmp1 buffers must hold:
+ * Zc*Yc*Xp + 64 with Xp = Xc rounded up to a multiple of 4. */
+int si_smooth_tmp_floats(int Zc, int Yc, int Xc, unsigned long long* n);
+
 /* Curvature smoothing (rw_small.py:114-137, gpu_kernels.py:118-183): for each
  * of the nol maps, iters steps of phi <- phi + 0.01 * kappa(phi) on the
- * interior, borders unchanged. maps holds uint32 hits on entry and float32
- * smoothed values (bit pattern) on exit. tmp0/tmp1: float32 scratch of
- * Zc*Yc*Xc each. */
+ * interior, borders unchanged; kappa in binary32 in the reference's
+ * expression order, the update as `update` (enum si_smooth_update). maps
+ * holds uint32 hits on entry and float32 smoothed values (bit pattern) on
+ * exit. tmp0/tmp1: 16-byte aligned float32 scratch of si_smooth_tmp_floats
+ * each. Only kernel launches and asynchronous memsets on `stream`; waits
+ * inside the kernels are bounded and record a give-up in the status that
+ * si_smooth_status reads. */
 int si_smooth(uint32_t* maps, float* tmp0, float* tmp1, int nol, int Zc,
-              int Yc, int Xc, int iters, void* stream);
+              int Yc, int Xc, int iters, int update, void* stream);
 
 /* si_smooth on float32 maps (in place); used for the hybrid's combined maps. */
 int si_smooth_f32(float* maps, float* tmp0, float* tmp1, int nol, int Zc,
-                  int Yc, int Xc, int iters, void* stream);
+                  int Yc, int Xc, int iters, int update, void* stream);
+
+/* Status of the smoothing kernels on the current device since the last call
+ * (0 = fine; non-zero: a kernel's wait on its shared-memory copies gave up
+ * and its output is incomplete). Synchronises `stream`, then clears the
+ * status. Returns SI_ERR_CUDA when the status is non-zero. No counterpart in
+ * the reference. */
+int si_smooth_status(int* status, void* stream);
+
+/* Spin limit of every bounded wait on an mbarrier in this library (TMA copies
+ * of the smoothing and tile-walker kernels); spins < 0 restores the default
+ * (2^26). Process-wide. A wait that runs out makes its kernel wait (bounded)
+ * for its copies in flight, record an error status and return. No
+ * counterpart in the reference; tests use it to make a wait run out. */
+int si_set_wait_limit(long long spins);
 
 /* ---- the reference large path's seed set (optional mode) ----
  * si_extract_seeds with an in-plane box [box_y0, box_y1) x [box_x0, box_x1)

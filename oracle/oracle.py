@@ -720,7 +720,10 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, smooth_iters=0, all
     """The reference's small path with the oracle walk.
 
     mode 'philox': the product's semantics (Philox stream, exp2 weights,
-    binary32 smoothing update). mode 'reference': the reference's own
+    binary32 smoothing update). mode 'refstream': the product's
+    rng='reference' semantics (the reference's binary32 MRG stream seeded per
+    seed as the CUDA walker does, the product's exp2 weights, the smoothing
+    update as given). mode 'reference': the reference's own
     randomness and arithmetic (binary32 MRG stream seeded per seed as the CUDA
     walker does, expf weights, binary64 smoothing update) — used to pin this
     restatement against the reference's outputs. seeding 'large': the
@@ -766,6 +769,8 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, smooth_iters=0, all
     if mode == "reference":
         hits = walk_c(data, seeds, nbrw, sorw, key, nol, rng="ref_mrg", weight="ref_expf",
                       rng_index=seeds.rng_cuda)
+    elif mode == "refstream":
+        hits = walk_c(data, seeds, nbrw, sorw, key, nol, rng="ref_mrg", weight="exp2", rng_index=seeds.rng_cuda)
     elif walker == "numpy":
         hits = walk_numpy(data, seeds, nbrw, sorw, key, nol)
     else:

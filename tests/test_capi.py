@@ -39,7 +39,7 @@ def test_argument_errors_without_launch(native_lib):
     rc = native_lib.si_walk(None, 0, 8, 8, 8, None, None, 0, 1, 1, 0, None, 1, 0, 0, 0, None)
     assert rc == 1
     assert b"null pointer" in native_lib.si_last_error()
-    rc = native_lib.si_smooth(None, None, None, 1, 4, 4, 4, 1, None)
+    rc = native_lib.si_smooth(None, None, None, 1, 4, 4, 4, 1, 0, None)
     assert rc == 1
     assert _native.SI_F32 == 5
 

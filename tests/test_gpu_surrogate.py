@@ -229,13 +229,13 @@ def test_smooth_f32_matches_oracle(cuda):
     maps = rng.random((3, 19, 23, 37)).astype(np.float32)
     maps[:, 5:9] *= 4.0
     t = torch.from_numpy(maps.copy()).to(cuda)
-    V = maps[0].size
-    tmp0 = torch.empty(V, dtype=torch.float32, device=cuda)
-    tmp1 = torch.empty(V, dtype=torch.float32, device=cuda)
+    from biomedisa_gb300.interpolation import smooth_buffers, smooth_check
+    tmp0, tmp1 = smooth_buffers(19, 23, 37, cuda)
     for iters in (1, 4):
         t.copy_(torch.from_numpy(maps))
-        nat.call("si_smooth_f32", t.data_ptr(), tmp0.data_ptr(), tmp1.data_ptr(), 3, 19, 23, 37, iters,
+        nat.call("si_smooth_f32", t.data_ptr(), tmp0.data_ptr(), tmp1.data_ptr(), 3, 19, 23, 37, iters, 0,
                  torch.cuda.current_stream().cuda_stream)
+        smooth_check()
         assert np.array_equal(t.cpu().numpy(), O.smooth(maps, iters, "f32")), iters
 
 
