@@ -62,9 +62,12 @@ WORKLOADS = {
                        "128^3 volumes (procedural and large-style), soft-target cross entropy, AdamW",
                   nbrw=10, sorw=4000, smooth=0, allaxis=False),
     "hybrid": dict(desc="hybrid vs plain on the large uint8 1024^3 volume (6 phases, labels every 12th z-slice, "
-                        "nbrw=10, sorw=4000, smooth=0): surrogate everywhere, walk from the seeds within 8 voxels "
-                        "of voxels with max p < 0.97 (grown by 2); yardstick = the full plain walk",
-                   nbrw=10, sorw=4000, smooth=0, allaxis=False, threshold=0.97, radius=8, coarse=4, grow=2),
+                        "nbrw=10, sorw=4000, smooth=100 in both arms): surrogate everywhere, walk from the seeds "
+                        "within 8 voxels of voxels with max p < 0.9 (grown by 2), then 100 smoothing iterations; "
+                        "yardstick = the full plain walk with the same smoothing",
+                   nbrw=10, sorw=4000, smooth=100, allaxis=False, threshold=0.9, radius=8, coarse=4, grow=2),
+    "hybrid_097": dict(desc="as hybrid, with the tighter uncertainty threshold max p < 0.97",
+                       nbrw=10, sorw=4000, smooth=100, allaxis=False, threshold=0.97, radius=8, coarse=4, grow=2),
     "geodesic": dict(desc="geodesic interpolation (geodis.geodesic_segment: lamb=1.0, 4 forward+backward raster "
                           "iterations per label) of the plain uint8 128^3 volume, labels 0..2 on every 10th z-slice",
                      nbrw=0, sorw=0, smooth=0, allaxis=False),
@@ -96,7 +99,7 @@ def make_batch_inputs(seed: int = 0, count: int = 32):
 def make_inputs(name: str, seed: int = 0):
     from biomedisa_gb300 import synthetic as S
 
-    if name in ("large_ref", "hybrid"):
+    if name in ("large_ref", "hybrid", "hybrid_097"):
         name = "large"
     if name == "geodesic":
         name = "plain"
@@ -333,7 +336,7 @@ def main():
     if args.workload == "train":
         run_train_bench(args, wl)
         return
-    if args.workload == "hybrid":
+    if args.workload in ("hybrid", "hybrid_097"):
         run_hybrid_bench(args, wl)
         return
     if args.workload == "geodesic":
@@ -744,18 +747,19 @@ def run_hybrid_bench(args, wl):
     torch.cuda.synchronize()
     plain_ms = ev[0].elapsed_time(ev[1])
     plain = res["regular"]
+    plain_smooth = res.get("smooth")
     plain_steps = job.total_steps()
     present = sorted(int(v) for v in np.unique(lab[::12]))
     del job, res
     torch.cuda.empty_cache()
     kw = dict(threshold=wl["threshold"], radius=wl["radius"], coarse=wl["coarse"], grow=wl["grow"],
-              nbrw=wl["nbrw"], sorw=wl["sorw"])
+              nbrw=wl["nbrw"], sorw=wl["sorw"], smooth=wl["smooth"])
     for _ in range(args.warmup):
         r, _ = SG.hybrid_interpolation(None, None, net, device_inputs=(img_t, icode, lab_t, lcode), **kw)
         del r
     torch.cuda.synchronize()
     l2buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    times, launches, st, dice = [], 0, {}, {}
+    times, launches, st, dice, dice_smooth = [], 0, {}, {}, {}
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
             flush_l2(l2buf)
@@ -771,6 +775,7 @@ def run_hybrid_bench(args, wl):
             times.append(s.elapsed_time(e))
             launches = launches_since(before, st["sweeps"])
             dice = SG.label_dice(r["regular"], plain, present)
+            dice_smooth = SG.label_dice(r["smooth"], plain_smooth, present) if plain_smooth is not None else {}
             del r
     ms = max_over_ranks(world, sum(times) / len(times))
     vox = int(np.prod(img.shape))
@@ -800,6 +805,9 @@ def run_hybrid_bench(args, wl):
         "plain_ms": plain_ms, "plain_voxels_per_s": vox / (plain_ms / 1e3), "speedup_vs_plain": plain_ms / ms,
         "dice_vs_plain": {str(k): round(v, 5) for k, v in dice.items()},
         "dice_min": min(dice.values()) if dice else None,
+        "dice_smooth_vs_plain": {str(k): round(v, 5) for k, v in dice_smooth.items()},
+        "dice_smooth_min": min(dice_smooth.values()) if dice_smooth else None,
+        "threshold": wl["threshold"],
         "frac_uncertain": st.get("frac_uncertain"), "frac_seeds_walked": st.get("frac_seeds_walked"),
         "walker_steps": st.get("walker_steps"), "plain_walker_steps": plain_steps,
         "seconds_surrogate": st.get("seconds_surrogate"), "seconds_walk": st.get("seconds_walk"),

@@ -24,7 +24,7 @@ NVCC_FLAGS = [
     "-std=c++17",
     "--fmad=false",  # no implicit contraction: fused ops only where written
     "-Xptxas",
-    "--fmad=false",  # nor in ptxas (packed .f32x2 products feeding packed sums)
+    "--fmad=false",  # nor in ptxas (packed products are kept apart separately: si_common.cuh f2_mul)
     "-Xcompiler",
     "-fPIC",
     "-Xptxas",

@@ -390,6 +390,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(const void* __restrict__ pac
   const size_t V = (size_t)g.F * g.Zc;
   const uint32_t stride = gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
+  const uint64_t nz = f2_negzero();
   // warp-uniform trip count, so the counting below runs with full warps
   const uint32_t i_end = (n_live + 31u) & ~31u;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < i_end; i += stride) {
@@ -402,7 +403,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(const void* __restrict__ pac
       const uint32_t t_end = min(st.z + K, te);
       uint32_t* __restrict__ hl = hits + (size_t)(st.w >> 24) * V;
       st.x = walk_steps<kFloat>(packed, st.x, st.z, t_end, sd.c, sd.b, sd.pos, seed_axis(sd.meta),
-                                seed_label(sd.meta), k0, k1, hl, s_delta);
+                                seed_label(sd.meta), k0, k1, hl, s_delta, nz);
       st.z = t_end;
       states[i] = st;
       alive = t_end != te;
@@ -860,6 +861,7 @@ __global__ void __launch_bounds__(256) bsweep_kernel(const VolDesc* __restrict__
   }
   __syncthreads();
   const uint32_t stride = gridDim.x * blockDim.x;
+  const uint64_t nz = f2_negzero();
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_live; i += stride) {
     uint4 st = states[i];
     const uint32_t v = bvol(st);
@@ -871,10 +873,10 @@ __global__ void __launch_bounds__(256) bsweep_kernel(const VolDesc* __restrict__
     uint32_t* __restrict__ hl = d.hits + (size_t)(st.w >> 24) * ((size_t)d.F * d.Zc);
     if (d.is_float)
       st.x = walk_steps<true>(d.packed, st.x, t, t_end, sd.c, sd.b, sd.pos, seed_axis(sd.meta), seed_label(sd.meta),
-                              k0, k1, hl, s_delta + 6 * v);
+                              k0, k1, hl, s_delta + 6 * v, nz);
     else
       st.x = walk_steps<false>(d.packed, st.x, t, t_end, sd.c, sd.b, sd.pos, seed_axis(sd.meta),
-                               seed_label(sd.meta), k0, k1, hl, s_delta + 6 * v);
+                               seed_label(sd.meta), k0, k1, hl, s_delta + 6 * v, nz);
     st.z = t_end | (st.z & 0xFF000000u);
     states[i] = st;
   }

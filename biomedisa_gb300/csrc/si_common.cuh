@@ -122,13 +122,21 @@ __device__ __forceinline__ float edge_weight(float d2, float c) {
 
 // ---------------------------------------------------------------------------
 // Two edge weights at once on the packed binary32 pipe of sm_100-class SMs
-// (add/sub/mul/fma.rn.f32x2: one instruction, two independent IEEE-754
+// (add/sub/fma.rn.f32x2: one instruction, two independent IEEE-754
 // round-to-nearest results). Each lane performs exactly the operation sequence
-// of edge_weight() above, so the pair equals two scalar calls bit for bit (the
-// library is built with ptxas contraction off, so a packed product is never
-// fused into a following packed sum). The walker is issue-bound and this
-// halves the floating-point instructions of its six weights. Operands travel
-// as 64-bit registers {lo, hi}.
+// of edge_weight() above, so the pair equals two scalar calls bit for bit. The
+// walker is issue-bound and this halves the floating-point instructions of its
+// six weights. Operands travel as 64-bit registers {lo, hi}.
+//
+// Products: ptxas fuses a packed mul.rn.f32x2 into a following packed add or
+// sub (one rounding instead of two), with or without --fmad=false, and it
+// also folds fma(a, b, -0.0) with a literal -0.0 back into that product. A
+// packed product is therefore written as fma(a, b, z) with z = -0.0 read at
+// run time from a mutable device variable (f2_negzero): RN(a*b + -0) equals
+// RN(a*b) for every input (signed zeros, infinities and NaN included), and an
+// FMA result cannot be fused further. Measured on the GB300: a mul->add chain
+// differed from the two-rounding sequence in 41 % of random pairs, every time
+// equal to the fused result; with the run-time -0 addend in none.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
   uint64_t r;
@@ -151,11 +159,6 @@ __device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
   asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
   return r;
 }
-__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
-  uint64_t r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
 __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
   uint64_t r;
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
@@ -163,12 +166,20 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
 }
 __device__ __forceinline__ uint64_t f2_splat(float v) { return f2_pack(v, v); }
 
+// -0.0 that neither compiler can see (read once per thread; see above).
+static __device__ float g_opaque_negzero = -0.0f;
+__device__ __forceinline__ uint64_t f2_negzero() {
+  return f2_splat(*static_cast<volatile float*>(&g_opaque_negzero));
+}
+// Packed product RN(a*b) that is never fused into a later sum; nz = f2_negzero().
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b, uint64_t nz) { return f2_fma(a, b, nz); }
+
 // Weights of the two neighbours whose (B - I) differences are the lanes of d;
 // cc = {c, c}. Returns w_lo, w_hi equal to edge_weight(d_lo^2, c) and
 // edge_weight(d_hi^2, c).
-__device__ __forceinline__ void edge_weight_pair(uint64_t d, uint64_t cc, float& w_lo, float& w_hi) {
+__device__ __forceinline__ void edge_weight_pair(uint64_t d, uint64_t cc, uint64_t nz, float& w_lo, float& w_hi) {
   const uint64_t magic2 = f2_splat(kRoundMagic);
-  const uint64_t y = f2_mul(f2_mul(d, d), cc);
+  const uint64_t y = f2_mul(f2_mul(d, d, nz), cc, nz);
   const uint64_t r = f2_add(y, magic2);
   const uint64_t g = f2_sub(f2_sub(r, magic2), y);
   uint64_t p = f2_fma(f2_splat(kP5), g, f2_splat(kP4));
@@ -224,7 +235,7 @@ __device__ __forceinline__ float byte_plus_2p23(uint32_t w, uint32_t k) {
 template <bool kFloat>
 __device__ __forceinline__ uint32_t walk_step_u(const void* __restrict__ packed_v, uint32_t pos, float u, float c,
                                                 float bf, float b23, uint32_t* __restrict__ hl,
-                                                const int32_t* s_delta) {
+                                                const int32_t* s_delta, uint64_t nz) {
   float w0, w1, w2, w3, w4, w5;
   uint32_t mask;
   // The (B - I) differences are formed pairwise (+z,-z), (+y,-y), (+x,-x) and
@@ -235,16 +246,16 @@ __device__ __forceinline__ uint32_t walk_step_u(const void* __restrict__ packed_
     const float4* rec = static_cast<const float4*>(packed_v) + 2 * (size_t)pos;
     const float4 a = rec[0], b = rec[1];
     const uint64_t bf2 = f2_splat(bf);
-    edge_weight_pair(f2_sub(bf2, f2_pack(a.x, a.y)), cc, w0, w1);
-    edge_weight_pair(f2_sub(bf2, f2_pack(a.z, a.w)), cc, w2, w3);
-    edge_weight_pair(f2_sub(bf2, f2_pack(b.x, b.y)), cc, w4, w5);
+    edge_weight_pair(f2_sub(bf2, f2_pack(a.x, a.y)), cc, nz, w0, w1);
+    edge_weight_pair(f2_sub(bf2, f2_pack(a.z, a.w)), cc, nz, w2, w3);
+    edge_weight_pair(f2_sub(bf2, f2_pack(b.x, b.y)), cc, nz, w4, w5);
     mask = __float_as_uint(b.z);
   } else {
     const uint2 r = static_cast<const uint2*>(packed_v)[pos];
     const uint64_t b2 = f2_splat(b23);
-    edge_weight_pair(f2_sub(b2, f2_pack(byte_plus_2p23(r.x, 0), byte_plus_2p23(r.x, 1))), cc, w0, w1);
-    edge_weight_pair(f2_sub(b2, f2_pack(byte_plus_2p23(r.x, 2), byte_plus_2p23(r.x, 3))), cc, w2, w3);
-    edge_weight_pair(f2_sub(b2, f2_pack(byte_plus_2p23(r.y, 0), byte_plus_2p23(r.y, 1))), cc, w4, w5);
+    edge_weight_pair(f2_sub(b2, f2_pack(byte_plus_2p23(r.x, 0), byte_plus_2p23(r.x, 1))), cc, nz, w0, w1);
+    edge_weight_pair(f2_sub(b2, f2_pack(byte_plus_2p23(r.x, 2), byte_plus_2p23(r.x, 3))), cc, nz, w2, w3);
+    edge_weight_pair(f2_sub(b2, f2_pack(byte_plus_2p23(r.y, 0), byte_plus_2p23(r.y, 1))), cc, nz, w4, w5);
     mask = r.y >> 16;
   }
   const float c1 = __fadd_rn(w0, w1);
@@ -266,8 +277,8 @@ __device__ __forceinline__ uint32_t walk_step_u(const void* __restrict__ packed_
 template <bool kFloat>
 __device__ __forceinline__ uint32_t walk_step(const void* __restrict__ packed_v, uint32_t pos, uint32_t bits, float c,
                                               float bf, float b23, uint32_t* __restrict__ hl,
-                                              const int32_t* s_delta) {
-  return walk_step_u<kFloat>(packed_v, pos, u01_from_bits(bits), c, bf, b23, hl, s_delta);
+                                              const int32_t* s_delta, uint64_t nz) {
+  return walk_step_u<kFloat>(packed_v, pos, u01_from_bits(bits), c, bf, b23, hl, s_delta, nz);
 }
 
 __device__ __forceinline__ uint32_t philox_word(const U4& r, uint32_t sub) {
@@ -281,24 +292,24 @@ template <bool kFloat>
 __device__ __forceinline__ uint32_t walk_steps(const void* __restrict__ packed_v, uint32_t pos, uint32_t t,
                                                uint32_t t_end, float c, float bf, uint32_t seed_pos,
                                                uint32_t axis, uint32_t label, uint32_t k0, uint32_t k1,
-                                               uint32_t* __restrict__ hl, const int32_t* s_delta) {
+                                               uint32_t* __restrict__ hl, const int32_t* s_delta, uint64_t nz) {
   const float b23 = __fadd_rn(bf, 8388608.0f);  // 2^23 + B, exact for uint8 B
   if ((t & 3u) && t < t_end) {
     const U4 rr = philox4x32_10(U4{t >> 2, seed_pos, axis, label}, k0, k1);
     for (; (t & 3u) && t < t_end; ++t)
-      pos = walk_step<kFloat>(packed_v, pos, philox_word(rr, t & 3u), c, bf, b23, hl, s_delta);
+      pos = walk_step<kFloat>(packed_v, pos, philox_word(rr, t & 3u), c, bf, b23, hl, s_delta, nz);
   }
   for (; t + 4u <= t_end; t += 4u) {
     const U4 rr = philox4x32_10(U4{t >> 2, seed_pos, axis, label}, k0, k1);
-    pos = walk_step<kFloat>(packed_v, pos, rr.x, c, bf, b23, hl, s_delta);
-    pos = walk_step<kFloat>(packed_v, pos, rr.y, c, bf, b23, hl, s_delta);
-    pos = walk_step<kFloat>(packed_v, pos, rr.z, c, bf, b23, hl, s_delta);
-    pos = walk_step<kFloat>(packed_v, pos, rr.w, c, bf, b23, hl, s_delta);
+    pos = walk_step<kFloat>(packed_v, pos, rr.x, c, bf, b23, hl, s_delta, nz);
+    pos = walk_step<kFloat>(packed_v, pos, rr.y, c, bf, b23, hl, s_delta, nz);
+    pos = walk_step<kFloat>(packed_v, pos, rr.z, c, bf, b23, hl, s_delta, nz);
+    pos = walk_step<kFloat>(packed_v, pos, rr.w, c, bf, b23, hl, s_delta, nz);
   }
   if (t < t_end) {
     const U4 rr = philox4x32_10(U4{t >> 2, seed_pos, axis, label}, k0, k1);
     for (; t < t_end; ++t)
-      pos = walk_step<kFloat>(packed_v, pos, philox_word(rr, t & 3u), c, bf, b23, hl, s_delta);
+      pos = walk_step<kFloat>(packed_v, pos, philox_word(rr, t & 3u), c, bf, b23, hl, s_delta, nz);
   }
   return pos;
 }

@@ -287,6 +287,7 @@ __global__ void __launch_bounds__(256, 3) smooth_tma_kernel(const __grid_constan
   }
   const uint64_t two = f2_splat(2.0f), half = f2_splat(0.5f), quarter = f2_splat(0.25f);
   const uint64_t eps = f2_splat(1e-10f), hundredth = f2_splat(0.01f);
+  const uint64_t nz = f2_negzero();  // products as fma(a, b, -0): never fused into a later sum
   const bool row_in = y < Yc, row_interior = y > 0 && y < Yc - 1;
   const bool a_in = row_in && xa < Xc, b_in = row_in && xb < Xc;
   const bool a_int = row_interior && xa > 0 && xa < Xc - 1, b_int = row_interior && xb > 0 && xb < Xc - 1;
@@ -301,24 +302,24 @@ __global__ void __launch_bounds__(256, 3) smooth_tma_kernel(const __grid_constan
       const uint64_t k_pm = f2_pack(C[ia + kBoxX - 1], C[ib + kBoxX - 1]);
       uint64_t p_c, p_xm, p_xp, p_ym, p_yp;  // plane z+1
       cross(pl[(k + 2) & 3], p_c, p_xm, p_xp, p_ym, p_yp);
-      const uint64_t c2 = f2_mul(two, c_c);
-      const uint64_t dx = f2_mul(f2_sub(c_xm, c_xp), half);
+      const uint64_t c2 = f2_mul(two, c_c, nz);
+      const uint64_t dx = f2_mul(f2_sub(c_xm, c_xp), half, nz);
       const uint64_t dxx = f2_add(f2_sub(c_xm, c2), c_xp);
-      const uint64_t dx2 = f2_mul(dx, dx);
-      const uint64_t dy = f2_mul(f2_sub(c_ym, c_yp), half);
+      const uint64_t dx2 = f2_mul(dx, dx, nz);
+      const uint64_t dy = f2_mul(f2_sub(c_ym, c_yp), half, nz);
       const uint64_t dyy = f2_add(f2_sub(c_ym, c2), c_yp);
-      const uint64_t dy2 = f2_mul(dy, dy);
-      const uint64_t dz = f2_mul(f2_sub(m_c, p_c), half);
+      const uint64_t dy2 = f2_mul(dy, dy, nz);
+      const uint64_t dz = f2_mul(f2_sub(m_c, p_c), half, nz);
       const uint64_t dzz = f2_add(f2_sub(m_c, c2), p_c);
-      const uint64_t dz2 = f2_mul(dz, dz);
-      const uint64_t dxy = f2_mul(f2_sub(f2_sub(f2_add(k_mm, k_pp), k_mp), k_pm), quarter);
-      const uint64_t dxz = f2_mul(f2_sub(f2_sub(f2_add(p_xm, m_xp), p_xp), m_xm), quarter);
-      const uint64_t dyz = f2_mul(f2_sub(f2_sub(f2_add(p_ym, m_yp), p_yp), m_ym), quarter);
-      uint64_t num = f2_add(f2_mul(dxx, f2_add(dy2, dz2)), f2_mul(dyy, f2_add(dx2, dz2)));
-      num = f2_add(num, f2_mul(dzz, f2_add(dx2, dy2)));
-      num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dx), dy), dxy));
-      num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dx), dz), dxz));
-      num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dy), dz), dyz));
+      const uint64_t dz2 = f2_mul(dz, dz, nz);
+      const uint64_t dxy = f2_mul(f2_sub(f2_sub(f2_add(k_mm, k_pp), k_mp), k_pm), quarter, nz);
+      const uint64_t dxz = f2_mul(f2_sub(f2_sub(f2_add(p_xm, m_xp), p_xp), m_xm), quarter, nz);
+      const uint64_t dyz = f2_mul(f2_sub(f2_sub(f2_add(p_ym, m_yp), p_yp), m_ym), quarter, nz);
+      uint64_t num = f2_add(f2_mul(dxx, f2_add(dy2, dz2), nz), f2_mul(dyy, f2_add(dx2, dz2), nz));
+      num = f2_add(num, f2_mul(dzz, f2_add(dx2, dy2), nz));
+      num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dx, nz), dy, nz), dxy, nz));
+      num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dx, nz), dz, nz), dxz, nz));
+      num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dy, nz), dz, nz), dyz, nz));
       const uint64_t den = f2_add(f2_add(f2_add(dx2, dy2), dz2), eps);
       float na, nb, da, db, ca, cb;
       f2_unpack(num, na, nb);
@@ -330,7 +331,7 @@ __global__ void __launch_bounds__(256, 3) smooth_tma_kernel(const __grid_constan
         oa = __double2float_rn(__dadd_rn((double)ca, __dmul_rn(0.01, (double)ka)));
         ob = __double2float_rn(__dadd_rn((double)cb, __dmul_rn(0.01, (double)kb)));
       } else {
-        f2_unpack(f2_add(c_c, f2_mul(hundredth, f2_pack(ka, kb))), oa, ob);
+        f2_unpack(f2_add(c_c, f2_mul(hundredth, f2_pack(ka, kb), nz)), oa, ob);
       }
       const bool z_int = z > 0 && z < Zc - 1;
       float* row = dst + (size_t)z * dF + (size_t)y * dst_pitch;

@@ -90,6 +90,7 @@ __global__ void __launch_bounds__(256) walk_kernel(const void* __restrict__ pack
   const uint32_t ns = min(*n_seeds_ptr, max_seeds);
   if (ns == 0) return;
   const uint64_t total = (uint64_t)ns * (uint32_t)nbrw;
+  const uint64_t nz = f2_negzero();
   const size_t V = (size_t)F * Zc;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t item = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; item < total; item += stride) {
@@ -105,7 +106,7 @@ __global__ void __launch_bounds__(256) walk_kernel(const void* __restrict__ pack
     uint32_t* __restrict__ hl = hits + (size_t)seed_slot(sd.meta) * V;
     const uint32_t t0 = n * (uint32_t)sorw;
     walk_steps<kFloat>(packed_v, sd.pos, t0, t0 + (uint32_t)sorw, sd.c, sd.b, sd.pos, seed_axis(sd.meta),
-                       seed_label(sd.meta), k0, k1, hl, s_delta);
+                       seed_label(sd.meta), k0, k1, hl, s_delta, nz);
   }
 }
 
@@ -137,6 +138,7 @@ __global__ void __launch_bounds__(128) walk_refstream_kernel(const void* __restr
   const uint32_t ns = min(*n_seeds_ptr, max_seeds);
   const size_t V = (size_t)F * Zc;
   const uint32_t stride = gridDim.x * blockDim.x;
+  const uint64_t nz = f2_negzero();
   for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += stride) {
     const SeedRec sd = seeds[s];
     const uint32_t z = sd.pos / F, rem = sd.pos - z * F;
@@ -156,7 +158,7 @@ __global__ void __launch_bounds__(128) walk_refstream_kernel(const void* __restr
     for (int w = 0; w < nbrw; ++w) {
       uint32_t pos = sd.pos;
       for (int t = 0; t < sorw; ++t)
-        pos = walk_step_u<kFloat>(packed_v, pos, ref_stream_next(r), sd.c, sd.b, b23, hl, s_delta);
+        pos = walk_step_u<kFloat>(packed_v, pos, ref_stream_next(r), sd.c, sd.b, b23, hl, s_delta, nz);
     }
   }
 }

@@ -193,7 +193,8 @@ def test_hybrid_gain_over_untrained(cuda):
     """What the network gains: after a short training run on walked volumes
     (32 samples, 1000 steps) the hybrid walks well under all of the seeds of a
     held-out 256^3 volume and still agrees with the plain walk (per-label
-    Dice), while an untrained network is unsure everywhere and saves nothing."""
+    Dice >= 0.99), while an untrained network is unsure everywhere and saves
+    nothing."""
     from biomedisa_gb300 import synthetic as syn
     from biomedisa_gb300.interpolation import DeviceJob, _IMG_DTYPES, _LAB_DTYPES, normalize_host_dtypes, upload
     img, lab, _ = syn.large_volume(seed=5, shape=(256, 256, 256), z_every=12)
@@ -217,7 +218,7 @@ def test_hybrid_gain_over_untrained(cuda):
     print("hybrid", st["frac_seeds_walked"], st["frac_uncertain"], dice)
     assert st["frac_seeds_walked"] < 0.75
     assert st["walker_steps"] < 0.75 * job.total_steps()
-    assert min(dice.values()) >= 0.97
+    assert min(dice.values()) >= 0.99
 
 
 def test_smooth_f32_matches_oracle(cuda):
