@@ -38,4 +38,8 @@ inline int dtype_size(int dtype) {
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// 16 -> 16 channel 3x3x3 convolution on the tensor cores (si_umma.cu).
+int conv16_umma(const void* x, const void* w, const float* bias, const void* residual, void* y, int N, int D, int H,
+                int W, int dil, int relu, int out_f32, cudaStream_t st);
+
 }  // namespace si

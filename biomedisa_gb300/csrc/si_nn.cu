@@ -668,6 +668,16 @@ extern "C" int si_nn_conv3d_fwd(const void* x, const void* w, const float* bias,
   return check_launch("si_nn_conv3d_fwd");
 }
 
+extern "C" int si_nn_conv16_tc(const void* x, const void* w, const float* bias, const void* residual, void* y, int N,
+                               int D, int H, int W, int dil, int relu, int out_f32, void* stream) {
+  clear_error();
+  if (!x || !w || !y) return set_error(SI_ERR_ARG, "si_nn_conv16_tc: null pointer");
+  if (N < 1 || D < 1 || H < 1 || W < 1) return set_error(SI_ERR_ARG, "si_nn_conv16_tc: bad shape");
+  if (((uintptr_t)x | (uintptr_t)w | (uintptr_t)y | (uintptr_t)residual) % 16)
+    return set_error(SI_ERR_ARG, "si_nn_conv16_tc: tensors must be 16-byte aligned");
+  return conv16_umma(x, w, bias, residual, y, N, D, H, W, dil, relu, out_f32, as_stream(stream));
+}
+
 extern "C" int si_nn_wgrad_partial_bytes(int N, int D, int H, int W, int cin, int cout, uint64_t* bytes) {
   clear_error();
   if (!bytes || N < 1 || D < 1 || H < 1 || W < 1 || cin < 1 || cout < 1)

@@ -59,23 +59,46 @@ class Conv:
     wf: torch.Tensor = None  # bf16 flipped copy for the data gradient
 
 
-def conv_fwd(x, conv: Conv, shape, relu, residual=None, out_f32=False):
+def umma_check():
+    """Raises when a tensor-core convolution's bounded wait gave up since the
+    last check (synchronises the current stream)."""
+    import ctypes
+
+    st = ctypes.c_int(0)
+    nat.call("si_nn_umma_status", ctypes.byref(st), _stream())
+
+
+def _tensor_core_ok(conv: Conv, tensor_core: bool) -> bool:
+    return tensor_core and conv.cin == 16 and conv.cout == 16 and conv.dil <= 8
+
+
+def conv_fwd(x, conv: Conv, shape, relu, residual=None, out_f32=False, tensor_core=False):
+    """y = relu?(conv(x) + b + residual). tensor_core: the 16 -> 16 layers on
+    the tcgen05 kernel (si_nn_conv16_tc) instead of mma.sync."""
     N, D, H, W = shape
     y = torch.empty((N, D, H, W, conv.cout), dtype=torch.float32 if out_f32 else BF16, device=x.device)
-    nat.call("si_nn_conv3d_fwd", _p(x), _p(conv.wb), _p(conv.b), _p(residual), _p(y), N, D, H, W, conv.cin,
-             conv.cout, conv.dil, int(relu), int(out_f32), _stream())
+    if _tensor_core_ok(conv, tensor_core):
+        nat.call("si_nn_conv16_tc", _p(x), _p(conv.wb), _p(conv.b), _p(residual), _p(y), N, D, H, W, conv.dil,
+                 int(relu), int(out_f32), _stream())
+    else:
+        nat.call("si_nn_conv3d_fwd", _p(x), _p(conv.wb), _p(conv.b), _p(residual), _p(y), N, D, H, W, conv.cin,
+                 conv.cout, conv.dil, int(relu), int(out_f32), _stream())
     return y
 
 
-def conv_dgrad(dy, conv: Conv, shape, residual=None):
+def conv_dgrad(dy, conv: Conv, shape, residual=None, tensor_core=False):
     """dX = conv(dY, W flipped) (+ residual added in the epilogue)."""
     N, D, H, W = shape
     if conv.wf is None:
         conv.wf = torch.empty_like(conv.wb)
     nat.call("si_nn_flip_weights", _p(conv.wb), _p(conv.wf), conv.cout, conv.cin, _stream())
     dx = torch.empty((N, D, H, W, conv.cin), dtype=BF16, device=dy.device)
-    nat.call("si_nn_conv3d_fwd", _p(dy), _p(conv.wf), None, _p(residual), _p(dx), N, D, H, W, conv.cout, conv.cin,
-             conv.dil, 0, 0, _stream())
+    if _tensor_core_ok(conv, tensor_core):
+        nat.call("si_nn_conv16_tc", _p(dy), _p(conv.wf), None, _p(residual), _p(dx), N, D, H, W, conv.dil, 0, 0,
+                 _stream())
+    else:
+        nat.call("si_nn_conv3d_fwd", _p(dy), _p(conv.wf), None, _p(residual), _p(dx), N, D, H, W, conv.cout,
+                 conv.cin, conv.dil, 0, 0, _stream())
     return dx
 
 
@@ -115,11 +138,12 @@ def relu_bwd(g, y, add=None):
 class SurrogateNet:
     """The network; parameters live on the current CUDA device."""
 
-    def __init__(self, channels=16, dilations=(1, 2, 4, 8), seed=0, device=None):
+    def __init__(self, channels=16, dilations=(1, 2, 4, 8), seed=0, device=None, tensor_core=False):
         if channels not in (16, 32):
             raise ValueError("channels must be 16 or 32")
         self.device = torch.device(device) if device else torch.device("cuda", torch.cuda.current_device())
         self.channels, self.dilations = channels, tuple(dilations)
+        self.tensor_core = bool(tensor_core)  # 16 -> 16 layers on the tcgen05 kernel
         g = torch.Generator(device="cpu").manual_seed(seed)
         self.convs = [self._make(IN_CH, channels, 1, g)]
         for d in self.dilations:
@@ -154,14 +178,15 @@ class SurrogateNet:
         """x: bf16 [N, D, H, W, 16] -> fp32 logits [N, D, H, W, 16]."""
         shape = tuple(x.shape[:4])
         acts = [x]
-        a = conv_fwd(x, self.convs[0], shape, relu=True)
+        tc = self.tensor_core
+        a = conv_fwd(x, self.convs[0], shape, relu=True, tensor_core=tc)
         acts.append(a)
         for i in range(len(self.dilations)):
             c1, c2 = self.convs[1 + 2 * i], self.convs[2 + 2 * i]
-            t = conv_fwd(a, c1, shape, relu=True)
-            a = conv_fwd(t, c2, shape, relu=True, residual=a)
+            t = conv_fwd(a, c1, shape, relu=True, tensor_core=tc)
+            a = conv_fwd(t, c2, shape, relu=True, residual=a, tensor_core=tc)
             acts += [t, a]
-        logits = conv_fwd(a, self.convs[-1], shape, relu=False, out_f32=True)
+        logits = conv_fwd(a, self.convs[-1], shape, relu=False, out_f32=True, tensor_core=tc)
         if keep:
             self._acts, self._shape = acts, shape
         return logits
@@ -171,16 +196,17 @@ class SurrogateNet:
         acts, shape = self._acts, self._shape
         head = self.convs[-1]
         conv_wgrad(acts[-1], dlogits, head, shape)
-        da = conv_dgrad(dlogits, head, shape)
+        tc = self.tensor_core
+        da = conv_dgrad(dlogits, head, shape, tensor_core=tc)
         for i in reversed(range(len(self.dilations))):
             c1, c2 = self.convs[1 + 2 * i], self.convs[2 + 2 * i]
             a_in, t, a_out = acts[1 + 2 * i], acts[2 + 2 * i], acts[3 + 2 * i]
             relu_bwd(da, a_out)                 # g = dL/d(pre-activation of the block output)
             conv_wgrad(t, da, c2, shape)
-            dt = conv_dgrad(da, c2, shape)
+            dt = conv_dgrad(da, c2, shape, tensor_core=tc)
             relu_bwd(dt, t)
             conv_wgrad(a_in, dt, c1, shape)
-            da = conv_dgrad(dt, c1, shape, residual=da)  # conv1^T(dt) + g through the skip
+            da = conv_dgrad(dt, c1, shape, residual=da, tensor_core=tc)  # conv1^T(dt) + g through the skip
         relu_bwd(da, acts[1])
         conv_wgrad(acts[0], da, self.convs[0], shape)
         self._acts = None
@@ -355,6 +381,7 @@ def predict(net: SurrogateNet, job, slab=None, slab_voxels=1 << 28) -> torch.Ten
         nat.call("si_nn_probs", _p(logits), b - a, cp.Yc, cp.Xc, zs - a, ze - a, nol, _p(probs), cp.Zc, zs,
                  _stream())
         del logits
+    umma_check()
     return probs
 
 
@@ -461,6 +488,7 @@ def train(net: SurrogateNet, samples, steps, batch=4, patch=96, lr=2e-3, seed=0,
         losses.append(tot)
         if log_every and step % log_every == 0:
             print(f"step {step}: loss {float(tot):.4f}", flush=True)
+    umma_check()
     return [float(v) for v in losses]
 
 

@@ -475,11 +475,33 @@ int si_geo_visit_order(int Z, int Y, int X, int fwd, int32_t* t_of_voxel);
  * Convolutions are 3x3x3, stride 1, zero padding = dilation. */
 
 /* y = relu?(conv(x, w) + bias + residual); bias/residual nullable; out_f32
- * selects an fp32 output. cin: multiple of 16; cout: 16, 32, 48 or 64. */
+ * selects an fp32 output. cin: multiple of 16; cout: 16, 32, 48 or 64.
+ * Runs on mma.sync (m16n8k16 bf16); for 16 -> 16 see also si_nn_conv16_tc. */
 int si_nn_conv3d_fwd(const void* x, const void* w, const float* bias,
                      const void* residual, void* y, int N, int D, int H,
                      int W, int cin, int cout, int dil, int relu, int out_f32,
                      void* stream);
+
+/* The 16 -> 16 convolution of si_nn_conv3d_fwd (same arguments without
+ * cin/cout; dil <= 8; 16-byte aligned tensors) on the 5th-generation tensor
+ * cores: tcgen05.mma (M = 128 voxels of an x-row, N = 16 output channels,
+ * K = 16 input channels per tap, fp32 accumulators in tensor memory) over
+ * input rows staged by TMA, one MMA per tap. Same results as
+ * si_nn_conv3d_fwd up to fp32 accumulation order. Selectable through
+ * SurrogateNet(tensor_core=True); on this network's 16-channel layers it is
+ * slower than the mma.sync path (measured), so that one is the default. No
+ * counterpart in the reference. */
+int si_nn_conv16_tc(const void* x, const void* w, const float* bias,
+                    const void* residual, void* y, int N, int D, int H, int W,
+                    int dil, int relu, int out_f32, void* stream);
+
+/* Status of the tensor-core convolution kernel (si_nn_conv16_tc) on the
+ * current device since the last call:
+ * 0 = fine; non-zero: a kernel's bounded wait on its copies or MMAs gave up
+ * and its output is incomplete. Synchronises `stream`, then clears the
+ * status; returns SI_ERR_CUDA when it was non-zero. No counterpart in the
+ * reference. */
+int si_nn_umma_status(int* status, void* stream);
 
 /* dw[27][cout][cin] += sum_v dy[v][co] x[v + off][ci]; db[cout] += sum_v dy
  * (db nullable). (cout, cin) in {16, 32}^2. With `partials` (cin = cout = 16

@@ -62,6 +62,67 @@ def test_conv_forward_dgrad_wgrad(cin, cout, dil, shape, cuda):
     assert _rel(c.gb.cpu().numpy().astype(np.float64), dy.reshape(-1, cout).sum(0)) < 1e-5
 
 
+@pytest.mark.parametrize("dil,shape", [(1, (1, 3, 4, 300)), (2, (2, 5, 3, 257)), (8, (1, 4, 6, 128)),
+                                       (4, (3, 2, 2, 1))])
+def test_conv16_tensor_core_rows(dil, shape, cuda):
+    """The 16 -> 16 convolution on the tcgen05 tensor cores (si_nn_conv16_tc)
+    in tiles of 128 voxels of an x-row (several tiles per CTA, partial last
+    tiles, rows shorter than a tile): forward with bias, residual and ReLU, and
+    the data gradient, against the float64 oracle and the mma.sync path."""
+    rng = np.random.default_rng(dil * 31 + shape[-1])
+    x = NO.bf16_round(rng.standard_normal(shape + (16,)))
+    c, w, b = _conv(16, 16, dil, rng, cuda)
+    xt = _bf(x, cuda)
+    y = S.conv_fwd(xt, c, shape, relu=False, out_f32=True, tensor_core=True)
+    exp = NO.conv_fwd(x, w, b, dil)
+    assert np.max(np.abs(_np(y) - exp)) <= 1e-4 * max(1.0, np.abs(exp).max())
+    res = NO.bf16_round(rng.standard_normal(shape + (16,)))
+    yb = S.conv_fwd(xt, c, shape, relu=True, residual=_bf(res, cuda), tensor_core=True)
+    expb = NO.bf16_round(np.maximum(exp + res, 0))
+    assert np.max(np.abs(_np(yb) - expb) / (np.abs(expb) + 1e-2)) <= 2 ** -7
+    dy = NO.bf16_round(rng.standard_normal(shape + (16,)))
+    dx = S.conv_dgrad(_bf(dy, cuda), c, shape, tensor_core=True)
+    assert _rel(_np(dx), NO.conv_dgrad(dy, w, dil)) < 1e-2
+    # the mma.sync path gives the same fp32 sums up to accumulation order
+    ym = S.conv_fwd(xt, c, shape, relu=False, out_f32=True)
+    assert np.max(np.abs(_np(ym) - _np(y))) <= 1e-5 * max(1.0, np.abs(exp).max())
+    _umma_ok()
+
+
+def _umma_ok():
+    import ctypes
+    from biomedisa_gb300 import _native as nat
+    st = ctypes.c_int(0)
+    nat.call("si_nn_umma_status", ctypes.byref(st), torch.cuda.current_stream().cuda_stream)
+
+
+def test_conv16_tensor_core_wait_runs_out(cuda):
+    """With the wait limit at 0 spins the tensor-core convolution's waits give
+    up at once: the kernel lets its copies and MMAs complete, frees its tensor
+    memory, and the status reports it; with the default limit restored the
+    same convolution is correct on the same context."""
+    import ctypes
+    from biomedisa_gb300 import _native as nat
+    rng = np.random.default_rng(4)
+    shape = (1, 3, 3, 200)
+    x = NO.bf16_round(rng.standard_normal(shape + (16,)))
+    c, w, b = _conv(16, 16, 1, rng, cuda)
+    xt = _bf(x, cuda)
+    stream = torch.cuda.current_stream().cuda_stream
+    nat.call("si_set_wait_limit", 0)
+    try:
+        S.conv_fwd(xt, c, shape, relu=False, out_f32=True, tensor_core=True)
+        st = ctypes.c_int(0)
+        rc = nat.lib().si_nn_umma_status(ctypes.byref(st), ctypes.c_void_p(stream))
+        assert rc == 2 and st.value == 1
+    finally:
+        nat.call("si_set_wait_limit", -1)
+    y = S.conv_fwd(xt, c, shape, relu=False, out_f32=True, tensor_core=True)
+    exp = NO.conv_fwd(x, w, b, 1)
+    assert np.max(np.abs(_np(y) - exp)) <= 1e-4 * max(1.0, np.abs(exp).max())
+    _umma_ok()
+
+
 @pytest.mark.parametrize("channels", [16, 32])
 def test_network_gradient_check(channels, cuda):
     """Whole network (stem, 2 residual blocks, head): loss, logits and every
@@ -259,3 +320,24 @@ def test_hybrid_smooth_and_keys(cuda):
     reached = plain["hits"].sum(0) > 0
     assert reached.mean() > 0.5
     assert np.array_equal(res["regular"].cpu().numpy()[reached], plain["regular"][reached])
+
+
+def test_network_tensor_core_matches_mma(cuda):
+    """SurrogateNet(tensor_core=True) runs its 16 -> 16 layers on tcgen05: its
+    logits and weight gradients match the mma.sync network's."""
+    rng = np.random.default_rng(12)
+    shape = (1, 10, 12, 140)
+    x = torch.from_numpy(rng.uniform(0, 1, shape + (16,)).astype(np.float32)).to(cuda).to(torch.bfloat16)
+    p = torch.from_numpy(rng.dirichlet(np.ones(3), size=shape).astype(np.float32)).to(cuda)
+    out = []
+    for tc in (False, True):
+        net = S.SurrogateNet(seed=6, tensor_core=tc)
+        logits = net.forward(x, keep=True)
+        _, dl = net.loss_and_grad(logits, p, None, 3)
+        net.zero_grad()
+        net.backward(dl)
+        out.append((_np(logits), [c.gw.cpu().numpy().astype(np.float64) for c in net.convs]))
+    assert _rel(out[1][0], out[0][0]) < 1e-2
+    for k in range(len(out[0][1])):
+        assert _rel(out[1][1][k], out[0][1][k]) < 3e-2, k
+    _umma_ok()
