@@ -94,6 +94,20 @@ _SIGNATURES = {
     "si_geo_scan_launches": [_c_int, _c_int, _c_int, ctypes.c_double, _c_int, _c_int, _c_void_p],
     "si_geo_select": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_void_p, _c_void_p],
     "si_geo_visit_order": [_c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_acwe_minmax": [_c_void_p, _c_int, *[_c_int] * 9, _c_void_p, _c_void_p],
+    "si_acwe_gather": [_c_void_p, _c_int, *[_c_int] * 7, _c_float, _c_float, _c_void_p, *[_c_int] * 9, _c_void_p,
+                       _c_void_p, _c_void_p],
+    "si_acwe_label_sums": [_c_void_p, _c_void_p, _c_u64, _c_void_p, _c_void_p],
+    "si_acwe_evolution": [_c_void_p, _c_void_p, _c_void_p, ctypes.c_double, _c_int, _c_int, _c_int, _c_void_p,
+                          _c_void_p],
+    "si_acwe_morph": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_void_p],
+    "si_acwe_curvop": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_acwe_scatter": [_c_void_p, *[_c_int] * 9, _c_void_p, _c_void_p],
+    "si_acwe_dist_init": [_c_void_p, _c_u64, _c_void_p, _c_void_p],
+    "si_acwe_refine_hist": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p,
+                            _c_void_p],
+    "si_acwe_refine_decide": [_c_void_p, _c_void_p, _c_int, _c_int, _c_void_p, _c_void_p],
+    "si_acwe_refine_apply": [_c_void_p, _c_void_p, _c_void_p, *[_c_int] * 9, _c_void_p, _c_void_p],
 }
 
 EXPORTED = ("si_version", "si_last_error", *_SIGNATURES)

@@ -642,8 +642,6 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
     """
     if data is None or labelData is None:
         raise NotImplementedError("loading volumes from files is outside this package; pass numpy arrays")
-    if acwe:
-        raise NotImplementedError("acwe post-processing is not implemented on this path")
     if not torch.cuda.is_available():
         raise RuntimeError("smart_interpolation needs a CUDA device; there is no CPU fallback")
     data = np.asarray(data)
@@ -669,6 +667,15 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
         from .postprocess import post_results
 
         post_results(res, clean, fill)
+    if acwe:
+        # rw_small.py:246-252: both activeContour calls on the working image
+        # (zero outside the crop) and the regular result
+        from .active_contour import Frame, acwe_results
+
+        cp = job.cplan
+        frame = Frame(job.work, nat.SI_F32 if job.work_is_float else nat.SI_U8, (cp.cz0, cp.cy0, cp.cx0),
+                      (cp.Zc, cp.Yc, cp.Xc))
+        res["acwe"], res["refined"] = acwe_results(frame, res["regular"], acwe_alpha, acwe_smooth, acwe_steps)
     # sanity check of rw_small.py:203-211 (Dice of the input slices vs result)
     mask = lab > 0
     gt = lab.to(torch.int32)
@@ -679,7 +686,7 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
         print('Warning: Bad result! Use "--allaxis" if you labeled axes other than the xy-plane.')
     if return_device:
         return res
-    return {k: v.cpu().numpy() for k, v in res.items()}
+    return {k: (v.cpu().numpy() if v is not None else None) for k, v in res.items()}
 
 
 def walk(data, slices, indices, indices_child, nbrw, sorw, name=None, ctx=None, queue=None, allx=False,

@@ -229,3 +229,23 @@ def screw_like_volume(seed=0, shape=(419, 492, 462), z_every=20):
     _paint_ellipsoid(truth, 2, (0.5 * Z, 0.3 * Y, 0.7 * X), (0.2 * Z, 0.12 * Y, 0.12 * X), _rotation(rng))
     img = _render(truth, (150, 210), 40, 12.0, rng)
     return img, sparse_labels(truth, z_every=z_every), truth
+
+
+def blob_volume(shape, seed, labels, centres, radii, noise, dtype=np.uint8, jitter=1.5):
+    """Image of bright/dark ellipsoids with noise, and a label volume of the
+    same ellipsoids with perturbed radii (a segmentation to be refined)."""
+    rng = np.random.default_rng(seed)
+    zz, yy, xx = np.meshgrid(*[np.arange(s, dtype=np.float64) for s in shape], indexing="ij")
+    img = np.full(shape, 60.0)
+    lab = np.zeros(shape, np.int32)
+    for k, (lv, c, r) in enumerate(zip(labels, centres, radii)):
+        d = ((zz - c[0]) / r[0]) ** 2 + ((yy - c[1]) / r[1]) ** 2 + ((xx - c[2]) / r[2]) ** 2
+        img[d <= 1.0] = 110.0 + 50.0 * k
+        rr = 1.0 + jitter * (rng.random(shape) - 0.5) / max(r)
+        lab[d <= rr] = lv
+    img += rng.normal(0.0, noise, shape)
+    if dtype == np.uint8:
+        img = np.clip(np.rint(img), 0, 255).astype(np.uint8)
+    else:
+        img = (img * 3.7 - 40.0).astype(dtype)
+    return img, lab

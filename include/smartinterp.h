@@ -552,6 +552,102 @@ int si_nn_features(const uint8_t* img, const int16_t* slot_map,
 int si_nn_probs(const float* logits, int Ds, int H, int W, int zb, int ze,
                 int nol, float* probs, int Zout, int zo, void* stream);
 
+/* ---- Active contour post-processing ('acwe' and 'refined') -------------
+ * Replaces activeContour (biomedisa/features/active_contour.py:109-202, the
+ * `acwe` option of smart_interpolation, rw_small.py:246-255 and
+ * rw_large.py:262-271), its refinement (:204-225) and curvop_numba.py:5-149.
+ * Everything works on the reference's crop: image and labels padded by one
+ * zero voxel (padded frame, interior 1..Z, 1..Y, 1..X) and cut to
+ * [cz0, cz0+cZ) x [cy0, ..) x [cx0, ..) (reduce_blocksize, :84-104; the host
+ * computes the box from si_slice_flags' bbox). D (image) and L (labels) are
+ * uint8 crops in C order.
+ * Sequence, acwe: si_acwe_minmax (non-uint8 image) -> si_acwe_gather ->
+ *   steps x (zero sums -> si_acwe_label_sums -> si_acwe_evolution ->
+ *   si_acwe_curvop for every label) -> si_acwe_scatter.
+ * Sequence, refined: si_acwe_minmax -> si_acwe_gather -> si_acwe_dist_init ->
+ *   si_geo_scan(dist, zero image, lamb 0.0, 1 iteration) ->
+ *   si_acwe_refine_hist -> si_acwe_refine_decide -> si_acwe_refine_apply. */
+
+/* mm[0] = min, mm[1] = max (float32 values) of the voxels of an image array
+ * that lie in the padded frame's interior; the array's voxel (a, b, c) is
+ * padded voxel (iz0 + a, iy0 + b, ix0 + c). The caller initialises mm to
+ * (+inf, -inf). img_to_uint8's amin/amax (biomedisa_helper.py:345-352).
+ * dtype: SI_U8, SI_I8, SI_U16, SI_I16, SI_I32 or SI_F32. */
+int si_acwe_minmax(const void* img, int dtype, int iZ, int iY, int iX, int iz0,
+                   int iy0, int ix0, int Z, int Y, int X, float* mm,
+                   void* stream);
+
+/* D and L of the crop (active_contour.py:154-170). L = labels (uint8, Z x Y x
+ * X) at interior voxels, 0 on the pad. D: the image value (0 outside the
+ * image array and on the pad); convert = 0 copies a uint8 image, convert = 1
+ * applies img_to_uint8: ((v - mn) / mx) * 255 in binary32, truncated, with
+ * mn = amin and mx = amax - amin of the image as the reference sees it. */
+int si_acwe_gather(const void* img, int dtype, int iZ, int iY, int iX, int iz0,
+                   int iy0, int ix0, int convert, float mn, float mx,
+                   const uint8_t* labels, int Z, int Y, int X, int cz0,
+                   int cy0, int cx0, int cZ, int cY, int cX, uint8_t* D,
+                   uint8_t* L, void* stream);
+
+/* sums[l] += voxels of label l, sums[256 + l] += their intensity sum
+ * (l = 0..255) over n voxels; sums zeroed by the caller. The label means of
+ * active_contour.py:191-195. */
+int si_acwe_label_sums(const uint8_t* D, const uint8_t* L, uint64_t n,
+                       unsigned long long* sums, void* stream);
+
+/* One evolution pass (curvop_numba.py:5-29) of the crop (Z, Y, X): out = L
+ * with every interior voxel relabelled to the label, among its own and its
+ * 27 neighbours', whose mean (float32(sum / count) from sums) is closest to
+ * its intensity; label 0's distance is scaled by alpha (binary64). out must
+ * not alias L. */
+int si_acwe_evolution(const uint8_t* L, const uint8_t* D,
+                      const unsigned long long* sums, double alpha, int Z,
+                      int Y, int X, uint8_t* out, void* stream);
+
+/* One erosion (erode = 1, curvop_numba.py:31-60) or dilation (erode = 0,
+ * :62-84) pass of `label` over the crop; dst must not alias src. */
+int si_acwe_morph(const uint8_t* src, int Z, int Y, int X, int label, int erode,
+                  uint8_t* dst, void* stream);
+
+/* curvop(L, steps, label) (curvop_numba.py:86-149): `steps` rounds, even
+ * rounds erosion then dilation, odd rounds dilation then erosion; the result
+ * is left in L (tmp: scratch of the crop's size). */
+int si_acwe_curvop(uint8_t* L, uint8_t* tmp, int Z, int Y, int X, int label,
+                   int steps, void* stream);
+
+/* out (Z, Y, X) = the crop L put back in the padded frame without the pad
+ * (active_contour.py:185-188); 0 outside the crop. */
+int si_acwe_scatter(const uint8_t* L, int cz0, int cy0, int cx0, int cZ,
+                    int cY, int cX, int Z, int Y, int X, uint8_t* out,
+                    void* stream);
+
+/* dist[i] = 100 where L[i] == 0, else 0 (active_contour.py:206-207). */
+int si_acwe_dist_init(const uint8_t* L, uint64_t n, float* dist, void* stream);
+
+/* Band histograms of the refinement: hist[z][class_lut[L]][D] counts the
+ * crop voxels of slice z with dist <= 10 (active_contour.py:209-210,
+ * 213-216); hist (Z x ncls x 256 uint32) zeroed by the caller; class_lut[256]
+ * maps a label value to its class (-1 = not counted). */
+int si_acwe_refine_hist(const float* dist, const uint8_t* D, const uint8_t* L,
+                        const int16_t* class_lut, int ncls, int Z, int Y,
+                        int X, uint32_t* hist, void* stream);
+
+/* lut[z][v] (Z x 256) from histograms of ncand + 1 classes: candidate j is
+ * label cand_label[j] in class j + 1 (class 0 holds the other labels). For
+ * every candidate in order (the reference's allLabels[1:]) whose band in
+ * slice z holds voxels of the label and of other labels, the Gaussian
+ * likelihoods of intensity v under the two band classes (mean, standard
+ * deviation clamped to >= 1) give cand_label[j] where p1 > p2, else 0; a
+ * later candidate overwrites the slice (active_contour.py:212-224). */
+int si_acwe_refine_decide(const uint32_t* hist, const uint8_t* cand_label,
+                          int ncand, int Z, uint8_t* lut, void* stream);
+
+/* Refined labels out (Z, Y, X): lut[slice][D] at crop voxels with dist <= 10,
+ * 0 elsewhere and outside the crop. */
+int si_acwe_refine_apply(const float* dist, const uint8_t* D,
+                         const uint8_t* lut, int cz0, int cy0, int cx0, int cZ,
+                         int cY, int cX, int Z, int Y, int X, uint8_t* out,
+                         void* stream);
+
 /* Measurement probes (no counterpart in the reference; used by bench.py for
  * the walker's roofline denominators). si_probe_l2_read reads `bytes` of buf
  * `reps` times with L1-bypassing 16-byte loads (sink: one uint32, almost never

@@ -142,8 +142,51 @@ def _numba_typed(f):
     result cast back to the input dtype, as numba's store into the
     uint8/float32 output does.
     geodesic_raster_scan (geodis.py:44-76) runs on float32 views that follow
-    numba's float32/float64 typing (_NumbaF32)."""
+    numba's float32/float64 typing (_NumbaF32).
+    Active contour (curvop_numba.py, active_contour.py):
+      * evolution (:5-29): numba types the Python float ``alpha`` as float64,
+        so ``alpha * abs(float32)`` is a binary64 product; under NumPy 2 a
+        Python float times an np.float32 stays float32. alpha is passed as an
+        np.float64, which restores the binary64 product.
+      * erosion / dilation (:31-84): numba computes ``start[...] - label`` and
+        the running sum in int64; on uint8 NumPy scalars they wrap modulo 256
+        (a plane sum of 256 would read as 0). The label volume is read through
+        an int64 copy; the stores into the uint8 output are unchanged.
+      * geodis (active_contour.py:45-81): the float32 map is read through a
+        _NumbaF32Array (float32 + float64 and float32 + int64 are binary64 in
+        numba, the minimum is stored rounded to float32)."""
     name = getattr(f, "__name__", "")
+    if name == "evolution":
+
+        def evolution(mean, A, data, alpha):
+            import numpy as np
+
+            return f(mean, A, data, np.float64(alpha))
+
+        evolution.__name__ = name
+        return evolution
+    if name in ("erosion", "dilation"):
+
+        def morph(start, final, P3, zsh, ysh, xsh, label):
+            import numpy as np
+
+            f(start.astype(np.int64), final, P3, zsh, ysh, xsh, int(label))
+            return start, final
+
+        morph.__name__ = name
+        return morph
+    if name == "geodis":
+
+        def geodis(c, sqrt2, sqrt3, iterations):
+            import numpy as np
+
+            if c.dtype != np.float32:
+                raise TypeError("the typed emulation covers a float32 map only")
+            f(_NumbaF32Array(c), sqrt2, sqrt3, iterations)
+            return c
+
+        geodis.__name__ = name
+        return geodis
     if name == "geodesic_raster_scan":
 
         def scan(img, c, lamb=1.0, iterations=4):

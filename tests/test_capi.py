@@ -86,12 +86,15 @@ def test_entry_points_need_a_device_without_cuda():
     if torch.cuda.is_available():
         pytest.skip("a CUDA device is present")
     from biomedisa_gb300 import geodis, smart_interpolation
+    from biomedisa_gb300.active_contour import activeContour
 
     img = np.zeros((4, 5, 6), np.uint8)
     lab = np.zeros(img.shape, np.int32)
     lab[1, 1:3, 1:3] = 1
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         smart_interpolation(img, lab)
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        activeContour(img, lab)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         geodis.geodesic_segment(img, lab)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
