@@ -123,9 +123,11 @@ def read_labeled_slices(arr):
     return idx, arr[idx].astype(np.int32) if idx else np.zeros((0,) + arr.shape[1:], np.int32)
 
 
-def _allx_ones(arr):
-    """The one-pixel-line removal of biomedisa_helper.py:1024-1037."""
-    ones = (arr != 0).astype(np.int8)
+def _allx_ones(arr, positive=False):
+    """The one-pixel-line removal of biomedisa_helper.py:1024-1037 (labels
+    != 0; positive=True: labels > 0, as the large path's reader,
+    :1082-1094)."""
+    ones = ((arr > 0) if positive else (arr != 0)).astype(np.int8)
     grad = np.zeros(arr.shape, np.int8)
     tmp = np.abs(ones[:, :-1] - ones[:, 1:])
     grad[:, :-1] += tmp
@@ -371,6 +373,74 @@ def large_slice_box(stack):
     return amin_y, amax_y, amin_x, amax_x
 
 
+def read_labeled_slices_allx_large(arr):
+    """biomedisa_helper.py:1082-1099: the slices keeping a positive label
+    after the one-pixel-line removal (no slice skipping)."""
+    ones = _allx_ones(arr, positive=True)
+    return [k for k in range(arr.shape[0]) if np.any(ones[k])]
+
+
+def large_allx_slice_list(lab):
+    """The all-axis large path's slices (rw_large.py:68-107 on one GPU):
+    (axis, index) for z-slices of the crop, then y- and x-slices read from the
+    swapped crops."""
+    t1 = np.ascontiguousarray(np.swapaxes(lab, 0, 1))
+    t2 = np.ascontiguousarray(np.swapaxes(t1, 0, 2))
+    return ([(0, k) for k in read_labeled_slices_allx_large(lab)] +
+            [(1, k) for k in read_labeled_slices_allx_large(t1)] +
+            [(2, k) for k in read_labeled_slices_allx_large(t2)])
+
+
+def large_allx_labels(work_labels, slice_list):
+    """Per axis, the cropped label volume as that axis' slice stack holds it
+    after reduceBlocksize (pycuda_large_allx.py:37-57): the stack's box is
+    taken over its labels other than 0 and -1 (slices whose such labels all
+    sit in column 0 do not count), grown by 100 and clamped in the stack's
+    (row, column) plane; the axis' slices read -1 outside it. Returns
+    ({axis: volume}, {axis: (r0, r1, c0, c1)})."""
+    vols, boxes = {}, {}
+    for axis in (0, 1, 2):
+        lab = np.array(work_labels, dtype=np.int32, copy=True)
+        idx = [k for a, k in slice_list if a == axis]
+        if idx:
+            stack = np.stack([_slice_view(lab, axis, k) for k in idx])
+            stack[stack == -1] = 0
+            r0, r1, c0, c1 = large_slice_box(stack)
+            for k in idx:
+                view = _slice_view(lab, axis, k)
+                view[:r0] = -1
+                view[r1:] = -1
+                view[:, :c0] = -1
+                view[:, c1:] = -1
+            boxes[axis] = (r0, r1, c0, c1)
+        vols[axis] = lab
+    return vols, boxes
+
+
+def adaptive_seed_mask_allx(large_labs, seeds):
+    """The all-axis large walker's adaptive test (pycuda_large_allx.py:513-533
+    and :683-703): as adaptive_seed_mask, in the (row, column) plane of the
+    seed's own slice (z-slices (y, x), y-slices (z, x), x-slices (z, y)),
+    with that axis' labels."""
+    keep = np.zeros(len(seeds), bool)
+    for i in range(len(seeds)):
+        axis = int(seeds.axis[i])
+        lab = large_labs[axis]
+        Z, Y, X = lab.shape
+        p = int(seeds.pos[i])
+        z, y, x = p // (Y * X), (p // X) % Y, p % X
+        s, r, c = ((z, y, x), (y, z, x), (x, z, y))[axis]
+        if (r + c) % 4 == 0:
+            keep[i] = True
+            continue
+        plane = _slice_view(lab, axis, s)
+        R, C = plane.shape
+        w = plane[max(1, r - 100):min(R - 1, r + 101), max(1, c - 100):min(C - 1, c + 101)]
+        own = int(seeds.label[i])
+        keep[i] = bool(np.any((w != own) & (w != -1)))
+    return keep
+
+
 def large_labels(work_labels, idx):
     """The cropped label volume as the large walker sees it: the taken
     z-slices with -1 outside their box (for seeds and their variance)."""
@@ -437,7 +507,7 @@ def extract_seeds(work_img, work_labels, slice_list, all_labels, var_mode="inpla
     cols = {k: [] for k in ("pos", "slot", "axis", "label", "b", "var", "rng_cuda", "rng_ocl")}
     stack_count = {0: 0, 1: 0, 2: 0}
     for axis, s in slice_list:
-        lab2 = _slice_view(work_labels, axis, s)
+        lab2 = _slice_view(work_labels[axis] if isinstance(work_labels, dict) else work_labels, axis, s)
         img2 = _slice_view(imgf, axis, s)
         R, C = lab2.shape
         stack_idx = stack_count[axis]
@@ -729,7 +799,10 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, smooth_iters=0, all
     restatement against the reference's outputs. seeding 'large': the
     reference large path's seed set (slice skipping, in-plane label box,
     adaptive seeds; biomedisa_helper.py:1068-1080, pycuda_large.py:39-58 and
-    :513-533) with the same walk."""
+    :513-533) with the same walk; with allaxis the all-axis large path's
+    (every slice with a positive label on each axis, a box per axis,
+    adaptive seeds in slice coordinates; biomedisa_helper.py:1082-1099,
+    rw_large.py:68-107, pycuda_large_allx.py:37-57 and :513-533)."""
     if mode == "reference":
         smooth_update = "ref_f64"
     labelData, allLabels = pre_processing(labelData, only, ignore)
@@ -746,7 +819,9 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, smooth_iters=0, all
     az, bz, ay, by, ax, bx = predict_blocksize(labelData)
     data = np.ascontiguousarray(data[az:bz, ay:by, ax:bx])
     lab = np.ascontiguousarray(labelData[az:bz, ay:by, ax:bx])
-    if allaxis:
+    if allaxis and seeding == "large":
+        slice_list = large_allx_slice_list(lab)
+    elif allaxis:
         sl = [(k, 0) for (k, _) in read_indices_allx(lab, 0)]
         t1 = np.ascontiguousarray(np.swapaxes(lab, 0, 1))
         sl += [(k, 1) for (k, _) in read_indices_allx(t1, 1)]
@@ -757,9 +832,11 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, smooth_iters=0, all
         slice_list = [(0, k) for k in read_labeled_slices_large(lab)]
     else:
         slice_list = [(0, k) for k in read_labeled_slices(lab)[0]]
-    if seeding == "large":
-        if allaxis:
-            raise ValueError("large-path seeding is restated for z-slices only")
+    if seeding == "large" and allaxis:
+        llabs, _ = large_allx_labels(lab, slice_list)
+        seeds = extract_seeds(data, llabs, slice_list, allLabels)
+        seeds = subset_seeds(seeds, adaptive_seed_mask_allx(llabs, seeds))
+    elif seeding == "large":
         llab, _ = large_labels(lab, [k for _, k in slice_list])
         seeds = extract_seeds(data, llab, slice_list, allLabels)
         seeds = subset_seeds(seeds, adaptive_seed_mask(llab, seeds))

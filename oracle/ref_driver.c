@@ -7,6 +7,7 @@
  * (blocks spread over OpenMP threads); an OpenCL NDRange becomes loops over
  * global ids. Kernels are called exactly as the reference launches them:
  *   walkers   pycuda_small.py:96-106, pycuda_small_allx.py:163-173,
+ *             pycuda_large_allx.py:393-400,
  *             pyopencl_small.py:124-132
  *   smoothing rw_small.py:104-125 (curvature then update, block (32,32,1))
  *   top-3 / uncertainty rw_small.py:155-161.
@@ -66,6 +67,18 @@ int ref_launch_walk_large(int variant, int gx, int gy, int gz, int segment, void
 int ref_launch_walk_allx(int variant, int gx, int gy, int gz, int axis, int segment, void* raw, int* slices,
                          float* a, int xsh, int ysh, int zsh, int* indices, int sorw, float* beta, int nbrw) {
   cuda_walk_allx_fn k = variant == 0 ? ref_cuda_walk_allx_i8 : ref_cuda_walk_allx_f32;
+  CUDA_LAUNCH_BEGIN(gx, gy, gz)
+  k(axis, segment, (float*)raw, slices, a, xsh, ysh, zsh, indices, sorw, beta, nbrw);
+  CUDA_LAUNCH_END
+  return 0;
+}
+
+/* pycuda_large_allx walker (adaptive seeds in slice coordinates), one axis per
+ * launch (pycuda_large_allx.py:393-400: block (32, 32, 1), grid (cols/32+1,
+ * rows/32+1, slices of the axis)). */
+int ref_launch_walk_large_allx(int variant, int gx, int gy, int gz, int axis, int segment, void* raw, int* slices,
+                               float* a, int xsh, int ysh, int zsh, int* indices, int sorw, float* beta, int nbrw) {
+  cuda_walk_allx_fn k = variant == 0 ? ref_cuda_walk_large_allx_i8 : ref_cuda_walk_large_allx_f32;
   CUDA_LAUNCH_BEGIN(gx, gy, gz)
   k(axis, segment, (float*)raw, slices, a, xsh, ysh, zsh, indices, sorw, beta, nbrw);
   CUDA_LAUNCH_END

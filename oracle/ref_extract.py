@@ -8,6 +8,7 @@ reference's kernel factories with stubbed pycuda/pyopencl
 JIT-compile into ``_ref/ref_sources.inc``, each wrapped in renaming macros:
   * pycuda_small._build_kernel_int8/_float32           (walkers, CUDA small path)
   * pycuda_small_allx._build_kernel_int8/_float32      (walkers, CUDA all-axis)
+  * pycuda_large_allx._build_kernel_int8/_float32      (walkers, CUDA all-axis large path: adaptive seeds)
   * pycuda_large._build_kernel_int8/_float32          (walkers, CUDA large path: adaptive seeds)
   * pyopencl_small._build_kernel('char'|'float','uchar') (walkers, OpenCL)
   * gpu_kernels._build_curvature_gpu/_build_update_gpu/_build_kernel_max/
@@ -42,6 +43,10 @@ _KERNELS = [
      "Funktion"),
     ("biomedisa.features.random_walk.pycuda_small_allx", "_build_kernel_float32", (), "ref_cuda_walk_allx_f32",
      "Funktion"),
+    ("biomedisa.features.random_walk.pycuda_large_allx", "_build_kernel_int8", (), "ref_cuda_walk_large_allx_i8",
+     "Funktion"),
+    ("biomedisa.features.random_walk.pycuda_large_allx", "_build_kernel_float32", (),
+     "ref_cuda_walk_large_allx_f32", "Funktion"),
     ("biomedisa.features.random_walk.pyopencl_small", "_build_kernel", ("char", "uchar"), "ref_ocl_walk_char",
      "randomWalk"),
     ("biomedisa.features.random_walk.pyopencl_small", "_build_kernel", ("float", "uchar"), "ref_ocl_walk_float",

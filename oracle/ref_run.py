@@ -70,9 +70,9 @@ class _Kernel:
         if "a[index] = 0;" in code and "Funktion(float *a, int xsh, int ysh)" in code:
             self.kind = "fill"
         elif "Funktion(int axis" in code:
-            self.kind = "walk_allx"
+            self.kind = "walk_large_allx" if "Adaptive random walks" in code else "walk_allx"
         elif "Funktion(int segment" in code:
-            self.kind = "walk"
+            self.kind = "walk_large" if "Adaptive random walks" in code else "walk"
         elif "curvature[index] = (dxx" in code:
             self.kind = "curvature"
         elif "phi[index] += 0.01" in code:
@@ -97,6 +97,10 @@ class _Kernel:
             lib.ref_launch_walk(self.variant, gx, gy, gz, *c)
         elif self.kind == "walk_allx":
             lib.ref_launch_walk_allx(self.variant, gx, gy, gz, *c)
+        elif self.kind == "walk_large":
+            lib.ref_launch_walk_large(self.variant, gx, gy, gz, *c)
+        elif self.kind == "walk_large_allx":
+            lib.ref_launch_walk_large_allx(self.variant, gx, gy, gz, *c)
         else:
             kind = {"curvature": 0, "update": 1, "max": 2, "uncertainty": 3}[self.kind]
             lib.ref_launch_post(kind, gx, gy, gz, *c)
@@ -131,6 +135,10 @@ def _memcpy_dtoh(dst, src):
     dst[...] = src.a.view(dst.dtype).reshape(dst.shape)
 
 
+def _memcpy_htod(dst, src):
+    dst.a.view(np.uint8).reshape(-1)[...] = np.frombuffer(np.ascontiguousarray(src).tobytes(), np.uint8)
+
+
 class _Comm:
     def Get_rank(self):
         return 0
@@ -147,6 +155,9 @@ class _Comm:
     def Barrier(self):
         pass
 
+    def Allreduce(self, send, recv, op=None):
+        recv[0][...] = send[0]
+
     def Split(self, color, key):
         return _Comm()
 
@@ -158,6 +169,7 @@ def _fakes():
     drv.Device = _Device
     drv.mem_alloc = lambda nbytes: FakeArray(np.zeros(int(nbytes), np.uint8))
     drv.memcpy_dtoh = _memcpy_dtoh
+    drv.memcpy_htod = _memcpy_htod
     ga = types.ModuleType("pycuda.gpuarray")
     ga.to_gpu = FakeArray
     ga.zeros = lambda shape, dtype=np.float32: FakeArray(np.zeros(shape, dtype))
@@ -175,17 +187,31 @@ def _fakes():
             "mpi4py.MPI": MPI}
 
 
-def reference_smart_interpolation(data, labelData, **kwargs):
-    """Calls the reference's smart_interpolation (CUDA small path) and returns
-    its result dict."""
+def reference_smart_interpolation(data, labelData, force_large=False, **kwargs):
+    """Calls the reference's smart_interpolation (CUDA path) and returns its
+    result dict. force_large=True sends the volume down the reference's large
+    path (rw_large.py, pycuda_large*.py) as a volume above its size threshold
+    would go (interpolation.py:196): the label count that pre_processing
+    reports is inflated after it returns, which only that test reads."""
     kwargs.setdefault("platform", "cuda_force")
     ref_lib()
     with reference_modules():
         saved = {k: sys.modules.get(k) for k in _fakes()}
         sys.modules.update(_fakes())
         try:
+            import biomedisa.interpolation as interp
             from biomedisa.interpolation import smart_interpolation
 
+            if force_large:
+                original = interp.pre_processing
+
+                def pre_processing(bm):
+                    bm = original(bm)
+                    if bm.success:
+                        bm.nol = 10 ** 12
+                    return bm
+
+                interp.pre_processing = pre_processing
             return smart_interpolation(data, labelData, **kwargs)
         finally:
             for k, v in saved.items():

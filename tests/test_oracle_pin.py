@@ -219,6 +219,57 @@ def test_large_seeding_matches_reference_large_kernel_live():
         assert np.array_equal(a, hits[s].astype(np.float32)), f"label {seg}"
 
 
+def _large_allx_case():
+    """Labels on z-slices 3 and 11, y-slice 15 and x-slice 400 of a
+    16 x 22 x 460 volume: label 1 fills every row of the slices over a span
+    wider than the 201-voxel window (so the adaptive test drops seeds there),
+    label 2 beyond it, a patch of -1 (ignored); uint8 image."""
+    lab = np.zeros((16, 22, 460), np.int32)
+    for z in (3, 11):
+        lab[z, :, :300] = 1
+        lab[z, :, 300:450] = 2
+    lab[11, 6:10, 40:70] = -1
+    lab[:, 15, :300] = 1
+    lab[:, 15, 300:420] = 2
+    lab[:, :, 400] = 2
+    lab[4:9, 5:12, 400] = 1
+    rng = np.random.default_rng(6)
+    img = (rng.normal(90, 20, lab.shape) + 60 * (lab == 2)).clip(0, 255).astype(np.uint8)
+    return img, lab
+
+
+@pytest.mark.skipif(not _ref_available(), reason="reference kernels not built")
+@pytest.mark.parametrize("allaxis", [False, True])
+def test_large_path_matches_reference_end_to_end_live(allaxis):
+    """The reference's own large path end to end — interpolation.py's
+    dispatch forced to rw_large.py, its slice readers, reduceBlocksize,
+    Beta, the large walkers (pycuda_large.py / pycuda_large_allx.py,
+    adaptive seeds) compiled as C, max_to_label and smoothing — against the
+    oracle's large seeding in the reference's arithmetic and stream."""
+    import ref_run
+
+    img, lab = (_large_allx_case() if allaxis else _large_case())
+    kw = dict(nbrw=2, sorw=40, allaxis=allaxis, smooth=3)
+    ref = ref_run.reference_smart_interpolation(img, lab, force_large=True, **kw)
+    exp = O.smart_interpolation(img, lab, nbrw=2, sorw=40, allaxis=allaxis, smooth_iters=3, mode="reference",
+                                seeding="large")
+    assert np.array_equal(ref["regular"], exp["regular"])
+    assert np.array_equal(ref["smooth"], exp["smooth"])
+    if allaxis:
+        assert {a for a, _ in exp["slice_list"]} == {0, 1, 2}
+        # the adaptive test dropped seeds on the axes whose planes are wider
+        # than the window (the x-slice plane is 18 x 24: all its seeds see
+        # both labels)
+        az, bz, ay, by, ax, bx = exp["crop"]
+        l2 = np.pad(lab, 1)[az:bz, ay:by, ax:bx]
+        llabs, _ = O.large_allx_labels(l2, exp["slice_list"])
+        d2 = np.ascontiguousarray(np.pad(O.normalize_image(img), 1)[az:bz, ay:by, ax:bx])
+        raw = O.extract_seeds(d2, llabs, exp["slice_list"], exp["allLabels"])
+        for a in range(2):
+            assert 0 < int((exp["seeds"].axis == a).sum()) < int((raw.axis == a).sum()), a
+        assert int((exp["seeds"].axis == 2).sum()) > 0
+
+
 def test_cpu_baseline_port_walks_the_reference_sample():
     """The reference arm's fallback (the oracle's restatement of the reference
     OpenCL walker, for hosts without oracle/_ref) walks the same seeds of a
