@@ -94,6 +94,12 @@ _SIGNATURES = {
     "si_geo_scan_launches": [_c_int, _c_int, _c_int, ctypes.c_double, _c_int, _c_int, _c_void_p],
     "si_geo_select": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_void_p, _c_void_p],
     "si_geo_visit_order": [_c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_extract_seeds_boxes": [_c_void_p, _c_int, *[_c_int] * 9, _c_void_p, _c_void_p, _c_void_p, _c_int, _c_void_p,
+                               _c_int, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p],
+    "si_adaptive_scratch_bytes_allx": [_c_int, _c_int, _c_int, _c_int, _c_void_p],
+    "si_adaptive_seed_filter_allx": [_c_void_p, _c_int, *[_c_int] * 9, _c_void_p, _c_void_p, _c_void_p, _c_int,
+                                     _c_void_p, _c_void_p, _c_void_p, _c_u32, _c_void_p, _c_void_p, _c_void_p, _c_u64,
+                                     _c_void_p],
     "si_acwe_minmax": [_c_void_p, _c_int, *[_c_int] * 9, _c_void_p, _c_void_p],
     "si_acwe_gather": [_c_void_p, _c_int, *[_c_int] * 7, _c_float, _c_float, _c_void_p, *[_c_int] * 9, _c_void_p,
                        _c_void_p, _c_void_p],

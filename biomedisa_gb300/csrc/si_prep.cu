@@ -60,11 +60,12 @@ struct LabelView {
   const T* lab;
   const uint8_t* nz_lut;  // shared-memory copy
   int Z0, Y0, X0;
+  bool neg_nz;  // negative values count as nonzero (labels != 0) or as zero (labels > 0)
   // nonzero test at ORIGINAL coordinates, zero outside.
   __device__ __forceinline__ bool nz(int z, int y, int x) const {
     if ((unsigned)z >= (unsigned)Z0 || (unsigned)y >= (unsigned)Y0 || (unsigned)x >= (unsigned)X0) return false;
     const int v = load_label(lab, ((uint64_t)z * Y0 + y) * X0 + x);
-    if (v < 0) return true;
+    if (v < 0) return neg_nz;
     if (v > 255) return false;
     return nz_lut[v] != 0;
   }
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(256) slice_flags_kernel(const T* __restrict__ 
   __shared__ uint8_t lut[256];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = nz_lut_g[i];
   __syncthreads();
-  LabelView<T> lv{lab, lut, Z0, Y0, X0};
+  LabelView<T> lv{lab, lut, Z0, Y0, X0, allaxis != 2};
   int bmin[3] = {INT_MAX, INT_MAX, INT_MAX};
   int bmax[3] = {-1, -1, -1};
   const uint64_t n = (uint64_t)Z0 * Y0 * X0;
@@ -308,6 +309,7 @@ extern "C" int si_slice_flags(const void* labels, int dtype, int Z0, int Y0, int
                               void* stream) {
   clear_error();
   if (!labels || !nz_lut || !flags_z || !bbox) return set_error(SI_ERR_ARG, "si_slice_flags: null pointer");
+  if (allaxis < 0 || allaxis > 2) return set_error(SI_ERR_ARG, "si_slice_flags: allaxis must be 0, 1 or 2");
   if (allaxis && (!flags_y || !flags_x)) return set_error(SI_ERR_ARG, "si_slice_flags: allaxis needs flags_y/flags_x");
   if (Z0 <= 0 || Y0 <= 0 || X0 <= 0) return set_error(SI_ERR_ARG, "si_slice_flags: bad dims");
   const uint64_t n = (uint64_t)Z0 * Y0 * X0;

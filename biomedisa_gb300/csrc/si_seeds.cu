@@ -19,7 +19,9 @@ struct SeedGeom {
   int cz0, cy0, cx0;
   int Zc, Yc, Xc;
   int max_rows;
-  int by0, by1, bx0, bx1;  // in-plane box (crop y, x); labels outside read as ignored (-1)
+  // per axis, the box [r0, r1) x [c0, c1) of the slice plane (rows, columns);
+  // labels outside it read as ignored (-1)
+  int box[3][4];
 };
 
 __device__ __forceinline__ int rows_of(const SeedGeom& g, int axis) { return axis == 0 ? g.Yc : g.Zc; }
@@ -41,9 +43,11 @@ struct SlotView {
   const T* lab;
   const int16_t* slot_lut;  // shared copy, 256 entries
   SeedGeom g;
-  // label slot at crop coordinates; -1 = no slot (negative label).
-  __device__ __forceinline__ int slot(int z, int y, int x) const {
-    if (y < g.by0 || y >= g.by1 || x < g.bx0 || x >= g.bx1) return -1;
+  // label slot at crop coordinates (z, y, x) = (row r, column c) of a slice
+  // of `axis`; -1 = no slot (negative label, or outside the axis' box).
+  __device__ __forceinline__ int slot(int axis, int r, int c, int z, int y, int x) const {
+    const int* b = g.box[axis];
+    if (r < b[0] || r >= b[1] || c < b[2] || c >= b[3]) return -1;
     const int oz = z + g.cz0 - 1, oy = y + g.cy0 - 1, ox = x + g.cx0 - 1;
     int v = 0;  // pad voxels carry label 0
     if ((unsigned)oz < (unsigned)g.Z0 && (unsigned)oy < (unsigned)g.Y0 && (unsigned)ox < (unsigned)g.X0)
@@ -63,7 +67,7 @@ __device__ __forceinline__ bool is_seed(const SlotView<T>& sv, int axis, int s, 
   int z, y, x;
   to_crop(axis, s, r, c, z, y, x);
   if (!interior(sv.g, z, y, x)) return false;
-  slot = sv.slot(z, y, x);
+  slot = sv.slot(axis, r, c, z, y, x);
   return slot >= 0;
 }
 
@@ -183,7 +187,7 @@ __global__ void __launch_bounds__(128) seed_emit_kernel(const T* __restrict__ la
           for (int o = -1; o <= 1; ++o) {
             int zz, yy, xx;
             to_crop(axis, s, r + n, c + o, zz, yy, xx);
-            if (sv.slot(zz, yy, xx) == slot) {
+            if (sv.slot(axis, r + n, c + o, zz, yy, xx) == slot) {
               const float tmp = __fsub_rn(b, img[(size_t)zz * F + (size_t)yy * g.Xc + xx]);
               dev = __fadd_rn(dev, __fmul_rn(tmp, tmp));
               summe = __fadd_rn(summe, 1.0f);
@@ -197,7 +201,7 @@ __global__ void __launch_bounds__(128) seed_emit_kernel(const T* __restrict__ la
           for (int o = -1; o <= 1; ++o) {
             int zz, yy, xx;
             to_crop(axis, s, r + n, c + o, zz, yy, xx);
-            if (sv.slot(zz, yy, xx) == slot) {
+            if (sv.slot(axis, r + n, c + o, zz, yy, xx) == slot) {
               const int d = bi - (int)img[(size_t)zz * F + (size_t)yy * g.Xc + xx];
               dev = __fadd_rn(dev, (float)(d * d));
               summe = __fadd_rn(summe, 1.0f);
@@ -226,8 +230,8 @@ using namespace si;
 static int extract_seeds_impl(const void* labels, int dtype, int Z0, int Y0, int X0, int cz0, int cy0, int cx0,
                               int Zc, int Yc, int Xc, const int16_t* slot_lut, const uint8_t* slot_label,
                               const void* work, int work_is_float, const int32_t* slice_list, int n_slices,
-                              uint32_t* row_counts, si_seed_t* seeds, uint32_t* n_seeds, int by0, int by1, int bx0,
-                              int bx1, void* stream) {
+                              uint32_t* row_counts, si_seed_t* seeds, uint32_t* n_seeds, const int32_t* boxes,
+                              void* stream) {
   if (!labels || !slot_lut || !slot_label || !work || !row_counts || !seeds || !n_seeds)
     return set_error(SI_ERR_ARG, "si_extract_seeds: null pointer");
   if (n_slices < 0 || (n_slices > 0 && !slice_list)) return set_error(SI_ERR_ARG, "si_extract_seeds: bad slice list");
@@ -241,7 +245,11 @@ static int extract_seeds_impl(const void* labels, int dtype, int Z0, int Y0, int
       return set_error(SI_ERR_CUDA, "si_extract_seeds: memset failed");
     return SI_OK;
   }
-  SeedGeom g{Z0, Y0, X0, cz0, cy0, cx0, Zc, Yc, Xc, Zc > Yc ? Zc : Yc, by0, by1, bx0, bx1};
+  SeedGeom g{Z0, Y0, X0, cz0, cy0, cx0, Zc, Yc, Xc, Zc > Yc ? Zc : Yc, {}};
+  for (int a = 0; a < 3; ++a) {
+    const int R = a == 0 ? Yc : Zc, C = a == 2 ? Yc : Xc;
+    for (int k = 0; k < 4; ++k) g.box[a][k] = boxes ? boxes[4 * a + k] : (k == 1 ? R : k == 3 ? C : 0);
+  }
   const dim3 grid(g.max_rows, n_slices);
   const uint32_t n = (uint32_t)((size_t)n_slices * g.max_rows);
   SeedRec* out = reinterpret_cast<SeedRec*>(seeds);
@@ -280,7 +288,7 @@ extern "C" int si_extract_seeds(const void* labels, int dtype, int Z0, int Y0, i
                                 uint32_t* row_counts, si_seed_t* seeds, uint32_t* n_seeds, void* stream) {
   clear_error();
   return extract_seeds_impl(labels, dtype, Z0, Y0, X0, cz0, cy0, cx0, Zc, Yc, Xc, slot_lut, slot_label, work,
-                            work_is_float, slice_list, n_slices, row_counts, seeds, n_seeds, 0, Yc, 0, Xc, stream);
+                            work_is_float, slice_list, n_slices, row_counts, seeds, n_seeds, nullptr, stream);
 }
 
 extern "C" int si_extract_seeds_box(const void* labels, int dtype, int Z0, int Y0, int X0, int cz0, int cy0,
@@ -290,9 +298,21 @@ extern "C" int si_extract_seeds_box(const void* labels, int dtype, int Z0, int Y
                                     int box_x1, uint32_t* row_counts, si_seed_t* seeds, uint32_t* n_seeds,
                                     void* stream) {
   clear_error();
+  // the box applies to z-slices (rows y, columns x); other axes keep their planes
+  const int32_t boxes[12] = {box_y0, box_y1, box_x0, box_x1, 0, Zc, 0, Xc, 0, Zc, 0, Yc};
   return extract_seeds_impl(labels, dtype, Z0, Y0, X0, cz0, cy0, cx0, Zc, Yc, Xc, slot_lut, slot_label, work,
-                            work_is_float, slice_list, n_slices, row_counts, seeds, n_seeds, box_y0, box_y1, box_x0,
-                            box_x1, stream);
+                            work_is_float, slice_list, n_slices, row_counts, seeds, n_seeds, boxes, stream);
+}
+
+extern "C" int si_extract_seeds_boxes(const void* labels, int dtype, int Z0, int Y0, int X0, int cz0, int cy0,
+                                      int cx0, int Zc, int Yc, int Xc, const int16_t* slot_lut,
+                                      const uint8_t* slot_label, const void* work, int work_is_float,
+                                      const int32_t* slice_list, int n_slices, const int32_t* boxes,
+                                      uint32_t* row_counts, si_seed_t* seeds, uint32_t* n_seeds, void* stream) {
+  clear_error();
+  if (!boxes) return set_error(SI_ERR_ARG, "si_extract_seeds_boxes: null boxes");
+  return extract_seeds_impl(labels, dtype, Z0, Y0, X0, cz0, cy0, cx0, Zc, Yc, Xc, slot_lut, slot_label, work,
+                            work_is_float, slice_list, n_slices, row_counts, seeds, n_seeds, boxes, stream);
 }
 
 // ---------------------------------------------------------------------------

@@ -209,9 +209,10 @@ class CropPlan:
     def voxels(self) -> int:
         return self.Zc * self.Yc * self.Xc
 
-    def seed_capacity(self) -> int:
+    def seed_capacity(self, slice_list=None) -> int:
         per = {0: self.Yc * self.Xc, 1: self.Zc * self.Xc, 2: self.Zc * self.Yc}
-        return int(sum(per[int(a)] for a, _ in self.slice_list))
+        sl = self.slice_list if slice_list is None else slice_list
+        return int(sum(per[int(a)] for a, _ in sl))
 
     @property
     def max_rows(self) -> int:
@@ -261,8 +262,6 @@ class DeviceJob:
             raise ValueError(f"walker must be one of {WALKERS}")
         if seeding not in SEEDINGS:
             raise ValueError(f"seeding must be one of {SEEDINGS}")
-        if seeding == "large" and allaxis:
-            raise ValueError("large-path seeding is supported for z-slices only (allaxis=False)")
         if smooth_update not in SMOOTH_UPDATES:
             raise ValueError(f"smooth_update must be one of {tuple(SMOOTH_UPDATES)}")
         self.smooth_update = smooth_update
@@ -344,13 +343,13 @@ class DeviceJob:
         nat.call("si_prepare_image", _ptr(self.img), self.img_code, *self.shape0, *cp.crop, float(mn), float(rng),
                  int(self.denoise), _ptr(self.work), _stream())
         self.launches += 1
-        cap = max(cp.seed_capacity(), 1)
+        slice_list = cp.slice_list
+        if self.seeding == "large":
+            slice_list = large_allx_slice_list(self) if self.allaxis else large_slice_list(cp.slice_list)
+        cap = max(cp.seed_capacity(slice_list), 1)
         self.seed_capacity = cap
         self.seeds = torch.empty(cap * SEED_RECORD_BYTES, dtype=torch.uint8, device=self.dev)
         self.n_seeds = torch.zeros(1, dtype=torch.int32, device=self.dev)
-        slice_list = cp.slice_list
-        if self.seeding == "large":
-            slice_list = large_slice_list(cp.slice_list)
         n_sl = len(slice_list)
         self.row_counts = torch.zeros(max(n_sl * cp.max_rows + 1, 1), dtype=torch.int32, device=self.dev)
         sl = torch.from_numpy(np.ascontiguousarray(slice_list.reshape(-1))).to(self.dev) if n_sl else \
@@ -384,6 +383,8 @@ class DeviceJob:
     def _large_seeds(self, slice_list, sl, slot_lut):
         """The reference large path's seed set: taken slices (slice_list),
         labels outside the in-plane box read as ignored, adaptive filter."""
+        if self.allaxis:
+            return self._large_allx_seeds(slice_list, sl, slot_lut)
         cp = self.cplan
         taken = [int(z) for _, z in slice_list.tolist()]
         self.large_box = large_slice_box(self, taken)
@@ -401,6 +402,32 @@ class DeviceJob:
         nat.call("si_adaptive_seed_filter", _ptr(self.lab), self.lab_code, *self.shape0, *cp.crop, _ptr(slot_lut),
                  _ptr(self.slot_label), _ptr(zs), n_sl, y0, y1, x0, x1, _ptr(raw), _ptr(n_raw), self.seed_capacity,
                  _ptr(self.seeds), _ptr(self.n_seeds), _ptr(scratch), int(need.value), _stream())
+        self.launches += 3 + 5
+
+    def _large_allx_seeds(self, slice_list, sl, slot_lut):
+        """The all-axis large path's seed set (rw_large.py:68-107 on one GPU,
+        pycuda_large_allx.py:309-322): every listed slice, one label box per
+        axis (labels outside read as ignored), adaptive filter in each
+        slice's own plane."""
+        cp = self.cplan
+        n_sl = len(slice_list)
+        boxes = np.zeros(12, np.int32)
+        for axis in range(3):
+            idx = [int(k) for a, k in slice_list.tolist() if a == axis]
+            boxes[4 * axis:4 * axis + 4] = large_plane_box(self, axis, idx, ignore_minus_one=True)
+        self.large_boxes = boxes.reshape(3, 4).copy()
+        raw = torch.empty_like(self.seeds)
+        n_raw = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        nat.call("si_extract_seeds_boxes", _ptr(self.lab), self.lab_code, *self.shape0, *cp.crop, _ptr(slot_lut),
+                 _ptr(self.slot_label), _ptr(self.work), int(self.work_is_float), _ptr(sl), n_sl,
+                 boxes.ctypes.data, _ptr(self.row_counts), _ptr(raw), _ptr(n_raw), _stream())
+        need = ctypes.c_uint64(0)
+        nat.call("si_adaptive_scratch_bytes_allx", cp.Zc, cp.Yc, cp.Xc, n_sl, ctypes.byref(need))
+        scratch = torch.empty(max(int(need.value), 1), dtype=torch.uint8, device=self.dev)
+        nat.call("si_adaptive_seed_filter_allx", _ptr(self.lab), self.lab_code, *self.shape0, *cp.crop,
+                 _ptr(slot_lut), _ptr(self.slot_label), _ptr(sl), n_sl, boxes.ctypes.data, _ptr(raw), _ptr(n_raw),
+                 self.seed_capacity, _ptr(self.seeds), _ptr(self.n_seeds), _ptr(scratch), int(need.value),
+                 _stream())
         self.launches += 3 + 5
 
     def walk(self):
@@ -520,20 +547,27 @@ def large_slice_list(slice_list: np.ndarray) -> np.ndarray:
     return np.asarray(out, np.int32).reshape(-1, 2)
 
 
-def large_slice_box(job, taken) -> tuple[int, int, int, int]:
-    """reduceBlocksize (pycuda_large.py:39-58) on the taken slices of the
-    crop: box of the non-zero labels of the slices whose non-zero voxels are
-    not all in crop column 0, grown by 100 voxels and clamped; (y0, y1, x0,
-    x1) in crop coordinates, labels outside read as -1."""
+def large_plane_box(job, axis, idx, ignore_minus_one=False) -> tuple[int, int, int, int]:
+    """reduceBlocksize on the stack of an axis' slices (crop indices idx):
+    the box of the labels other than 0 (and -1 with ignore_minus_one, as
+    pycuda_large_allx.py:37-57 zeroes -1 first; pycuda_large.py:39-58 does
+    not) of the slices whose such labels are not all in column 0, grown by 100
+    and clamped; (r0, r1, c0, c1) in the slice plane's crop coordinates (z-
+    slices: rows y, columns x; y-slices: rows z, columns x; x-slices: rows z,
+    columns y). Labels outside the box read as -1."""
     cp = job.cplan
-    Z0, Y0, X0 = job.shape0
-    Yc, Xc = cp.Yc, cp.Xc
-    amin_x, amax_x, amin_y, amax_y = Xc, 0, Yc, 0
-    if taken:
-        oy, ox = cp.cy0 - 1, cp.cx0 - 1
-        ys, ye, xs, xe = max(oy, 0), min(oy + Yc, Y0), max(ox, 0), min(ox + Xc, X0)
-        oz = torch.tensor([z + cp.cz0 - 1 for z in taken], dtype=torch.int64, device=job.dev)
-        v = job.lab.index_select(0, oz)[:, ys:ye, xs:xe].to(torch.int32)
+    dims_c = (cp.Zc, cp.Yc, cp.Xc)
+    offs = (cp.cz0 - 1, cp.cy0 - 1, cp.cx0 - 1)
+    dims0 = job.shape0
+    ra, ca = {0: (1, 2), 1: (0, 2), 2: (0, 1)}[axis]
+    R, C = dims_c[ra], dims_c[ca]
+    amin_c, amax_c, amin_r, amax_r = C, 0, R, 0
+    orig = [k + offs[axis] for k in idx if 0 <= k + offs[axis] < dims0[axis]]  # pad slices hold no label
+    if orig:
+        rs, re = max(offs[ra], 0), min(offs[ra] + R, dims0[ra])
+        cs, ce = max(offs[ca], 0), min(offs[ca] + C, dims0[ca])
+        o = torch.tensor(orig, dtype=torch.int64, device=job.dev)
+        v = job.lab.index_select(axis, o).movedim(axis, 0)[:, rs:re, cs:ce].to(torch.int32)
         eff_lut = np.zeros(256, np.int32)
         for k in range(256):
             slot = int(job.lplan.slot_lut[k])
@@ -541,21 +575,53 @@ def large_slice_box(job, taken) -> tuple[int, int, int, int]:
         lut = torch.from_numpy(eff_lut).to(job.dev)
         eff = torch.where(v < 0, v, torch.where(v > 255, torch.zeros_like(v), lut[v.clamp(0, 255).long()]))
         nz = eff != 0
-        xcoord = torch.arange(xs - ox, xe - ox, device=job.dev)  # crop columns of the loaded ones
-        qual = (nz & (xcoord != 0)[None, None, :]).flatten(1).any(1)
+        if ignore_minus_one:
+            nz &= eff != -1
+        ccoord = torch.arange(cs - offs[ca], ce - offs[ca], device=job.dev)  # crop columns of the loaded ones
+        qual = (nz & (ccoord != 0)[None, None, :]).flatten(1).any(1)
         nzq = nz & qual[:, None, None]
         rows = nzq.any(2).any(0)
         cols = nzq.any(1).any(0)
         if bool(rows.any()):
             ry = torch.nonzero(rows).flatten()
             cx = torch.nonzero(cols).flatten()
-            amin_y, amax_y = int(ry[0]) + ys - oy, int(ry[-1]) + ys - oy
-            amin_x, amax_x = int(cx[0]) + xs - ox, int(cx[-1]) + xs - ox
-    amin_x = amin_x - 100 if amin_x - 100 > 0 else 0
-    amax_x = amax_x + 100 if amax_x + 100 < Xc else Xc
-    amin_y = amin_y - 100 if amin_y - 100 > 0 else 0
-    amax_y = amax_y + 100 if amax_y + 100 < Yc else Yc
-    return amin_y, amax_y, amin_x, amax_x
+            amin_r, amax_r = int(ry[0]) + rs - offs[ra], int(ry[-1]) + rs - offs[ra]
+            amin_c, amax_c = int(cx[0]) + cs - offs[ca], int(cx[-1]) + cs - offs[ca]
+    amin_c = amin_c - 100 if amin_c - 100 > 0 else 0
+    amax_c = amax_c + 100 if amax_c + 100 < C else C
+    amin_r = amin_r - 100 if amin_r - 100 > 0 else 0
+    amax_r = amax_r + 100 if amax_r + 100 < R else R
+    return amin_r, amax_r, amin_c, amax_c
+
+
+def large_slice_box(job, taken) -> tuple[int, int, int, int]:
+    """reduceBlocksize (pycuda_large.py:39-58) on the taken z-slices of the
+    crop: (y0, y1, x0, x1) in crop coordinates, labels outside read as -1."""
+    return large_plane_box(job, 0, taken)
+
+
+def large_allx_slice_list(job) -> np.ndarray:
+    """The all-axis large path's slices (rw_large.py:68-107, one GPU): for
+    each axis the slices of the crop that keep a positive label after the
+    one-pixel-line removal (read_labeled_slices_allx_large,
+    biomedisa_helper.py:1082-1099; no skipping); (axis, crop index) pairs,
+    z-slices first."""
+    cp = job.cplan
+    Z0, Y0, X0 = job.shape0
+    fz = torch.zeros(Z0 + 2, dtype=torch.uint8, device=job.dev)
+    fy = torch.zeros(Y0 + 2, dtype=torch.uint8, device=job.dev)
+    fx = torch.zeros(X0 + 2, dtype=torch.uint8, device=job.dev)
+    imax = np.iinfo(np.int32).max
+    bbox = torch.tensor([imax, -1, imax, -1, imax, -1], dtype=torch.int32, device=job.dev)
+    nz = torch.from_numpy(job.lplan.nz_lut).to(job.dev)
+    nat.call("si_slice_flags", _ptr(job.lab), job.lab_code, Z0, Y0, X0, _ptr(nz), 2, _ptr(fz), _ptr(fy), _ptr(fx),
+             _ptr(bbox), _stream())
+    job.launches += 1
+    flags = [f.cpu().numpy() for f in (fz, fy, fx)]
+    offs = (cp.cz0, cp.cy0, cp.cx0)
+    lims = (cp.cz0 + cp.Zc, cp.cy0 + cp.Yc, cp.cx0 + cp.Xc)
+    out = [(a, int(k) - offs[a]) for a in range(3) for k in np.nonzero(flags[a])[0] if offs[a] <= k < lims[a]]
+    return np.asarray(out, np.int32).reshape(-1, 2)
 
 
 def pack_neighbours(work: torch.Tensor, is_float: bool, Zc: int, Yc: int, Xc: int) -> torch.Tensor:

@@ -90,6 +90,9 @@ int si_label_histogram(const void* labels, int dtype, uint64_t n,
  * allaxis = 1: flags_{z,y,x}[k] = 1 iff slice k of that axis keeps a nonzero
  *   pixel after removing one-pixel-wide lines (the gradient test of
  *   read_indices_allx / read_labeled_slices_allx, biomedisa_helper.py:1024-1066).
+ * allaxis = 2: as 1 with negative values counting as zero, for flags and
+ *   bbox (the large path's reader read_labeled_slices_allx_large,
+ *   biomedisa_helper.py:1082-1099, tests labels > 0).
  * bbox[6] = (zmin, zmax, ymin, ymax, xmin, xmax) in padded coordinates; the
  * caller initialises it to (INT_MAX, -1, INT_MAX, -1, INT_MAX, -1)
  * (predict_blocksize before the +-100 margin, biomedisa_helper.py:1105-1116).
@@ -350,6 +353,21 @@ int si_extract_seeds_box(const void* labels, int dtype, int Z0, int Y0, int X0,
                          uint32_t* row_counts, si_seed_t* seeds,
                          uint32_t* n_seeds, void* stream);
 
+/* si_extract_seeds with a box per axis: boxes (HOST array of 12 int32) holds
+ * for axis a = 0, 1, 2 the box [r0, r1) x [c0, c1) of that axis' slice plane
+ * in crop coordinates (z-slices: rows y, columns x; y-slices: rows z,
+ * columns x; x-slices: rows z, columns y) outside which labels read as
+ * ignored (-1): the all-axis large path's slice stacks after reduceBlocksize
+ * (pycuda_large_allx.py:37-57, one box per axis, :309-322). */
+int si_extract_seeds_boxes(const void* labels, int dtype, int Z0, int Y0,
+                           int X0, int cz0, int cy0, int cx0, int Zc, int Yc,
+                           int Xc, const int16_t* slot_lut,
+                           const uint8_t* slot_label, const void* work,
+                           int work_is_float, const int32_t* slice_list,
+                           int n_slices, const int32_t* boxes,
+                           uint32_t* row_counts, si_seed_t* seeds,
+                           uint32_t* n_seeds, void* stream);
+
 /* Adaptive seeds (pycuda_large.py:513-533): copies to seeds_out (count in
  * *n_out) the z-slice seeds of seeds_in (*n_in of at most max_in) with
  * (row + column) % 4 == 0 or a label other than their own and -1 within the
@@ -368,6 +386,26 @@ int si_adaptive_seed_filter(const void* labels, int dtype, int Z0, int Y0,
                             si_seed_t* seeds_out, uint32_t* n_out,
                             void* scratch, uint64_t scratch_bytes,
                             void* stream);
+
+/* Adaptive seeds of the all-axis large path (pycuda_large_allx.py:513-533 and
+ * :683-703): as si_adaptive_seed_filter for seeds of every axis, each tested
+ * in the (row, column) plane of its own slice (axis from the seed's meta
+ * bits 8-9) with that axis' box. slice_list: n_slices (axis, index) pairs in
+ * crop coordinates (device); boxes: HOST array of 12 int32 as for
+ * si_extract_seeds_boxes. Scratch: si_adaptive_scratch_bytes_allx. */
+int si_adaptive_scratch_bytes_allx(int Zc, int Yc, int Xc, int n_slices,
+                                   uint64_t* bytes);
+int si_adaptive_seed_filter_allx(const void* labels, int dtype, int Z0, int Y0,
+                                 int X0, int cz0, int cy0, int cx0, int Zc,
+                                 int Yc, int Xc, const int16_t* slot_lut,
+                                 const uint8_t* slot_label,
+                                 const int32_t* slice_list, int n_slices,
+                                 const int32_t* boxes,
+                                 const si_seed_t* seeds_in,
+                                 const uint32_t* n_in, uint32_t max_in,
+                                 si_seed_t* seeds_out, uint32_t* n_out,
+                                 void* scratch, uint64_t scratch_bytes,
+                                 void* stream);
 
 /* ---- outlier removal and hole filling (remove_outlier.py:67-141) ----
  * uint8 label volumes (Z, Y, X), at most 2^31 - 1 voxels; 6-connected

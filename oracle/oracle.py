@@ -417,27 +417,50 @@ def large_allx_labels(work_labels, slice_list):
     return vols, boxes
 
 
+def _window_count(mask, r, c):
+    """For each (r[i], c[i]): the number of True entries of the 2-D mask in
+    rows max(1, r-100)..min(R-2, r+100) and columns max(1, c-100)..min(C-2,
+    c+100) (the adaptive window clipped to the plane's interior), from an
+    integral image."""
+    R, C = mask.shape
+    ii = np.zeros((R + 1, C + 1), np.int64)
+    ii[1:, 1:] = mask.astype(np.int64).cumsum(0).cumsum(1)
+    r0, r1 = np.maximum(1, r - 100), np.minimum(R - 2, r + 100) + 1
+    c0, c1 = np.maximum(1, c - 100), np.minimum(C - 2, c + 100) + 1
+    return ii[r1, c1] - ii[r0, c1] - ii[r1, c0] + ii[r0, c0]
+
+
+def _adaptive_keep(plane, r, c, own):
+    """Seeds at (r, c) of one slice plane with labels own: kept iff
+    (r + c) % 4 == 0 or the window holds a label other than own and -1
+    (count of non-(-1) labels minus count of own labels > 0)."""
+    keep = (r + c) % 4 == 0
+    other = _window_count(plane != -1, r, c)
+    for v in np.unique(own):
+        sel = own == v
+        other[sel] -= _window_count(plane == v, r[sel], c[sel])
+    return keep | (other > 0)
+
+
 def adaptive_seed_mask_allx(large_labs, seeds):
     """The all-axis large walker's adaptive test (pycuda_large_allx.py:513-533
     and :683-703): as adaptive_seed_mask, in the (row, column) plane of the
     seed's own slice (z-slices (y, x), y-slices (z, x), x-slices (z, y)),
     with that axis' labels."""
     keep = np.zeros(len(seeds), bool)
-    for i in range(len(seeds)):
-        axis = int(seeds.axis[i])
-        lab = large_labs[axis]
-        Z, Y, X = lab.shape
-        p = int(seeds.pos[i])
-        z, y, x = p // (Y * X), (p // X) % Y, p % X
-        s, r, c = ((z, y, x), (y, z, x), (x, z, y))[axis]
-        if (r + c) % 4 == 0:
-            keep[i] = True
-            continue
-        plane = _slice_view(lab, axis, s)
-        R, C = plane.shape
-        w = plane[max(1, r - 100):min(R - 1, r + 101), max(1, c - 100):min(C - 1, c + 101)]
-        own = int(seeds.label[i])
-        keep[i] = bool(np.any((w != own) & (w != -1)))
+    if not len(seeds):
+        return keep
+    Z, Y, X = next(iter(large_labs.values())).shape
+    p = seeds.pos.astype(np.int64)
+    z, y, x = p // (Y * X), (p // X) % Y, p % X
+    axis = seeds.axis.astype(np.int64)
+    own = seeds.label.astype(np.int64)
+    coords = {0: (z, y, x), 1: (y, z, x), 2: (x, z, y)}
+    for a in (0, 1, 2):
+        sa, ra, ca = coords[a]
+        for s in np.unique(sa[axis == a]):
+            sel = (axis == a) & (sa == s)
+            keep[sel] = _adaptive_keep(_slice_view(large_labs[a], a, int(s)), ra[sel], ca[sel], own[sel])
     return keep
 
 
@@ -462,18 +485,7 @@ def adaptive_seed_mask(large_lab, seeds):
     iff (row + column) % 4 == 0 or its in-slice window [-100, 100]^2, clipped
     to the interior rows/columns 1..n-2, holds a label that is neither its own
     nor -1. Rows/columns are crop coordinates; large_lab from large_labels."""
-    Z, Y, X = large_lab.shape
-    keep = np.zeros(len(seeds), bool)
-    for i in range(len(seeds)):
-        p = int(seeds.pos[i])
-        z, y, x = p // (Y * X), (p // X) % Y, p % X
-        if (y + x) % 4 == 0:
-            keep[i] = True
-            continue
-        w = large_lab[z, max(1, y - 100):min(Y - 1, y + 101), max(1, x - 100):min(X - 1, x + 101)]
-        own = int(seeds.label[i])
-        keep[i] = bool(np.any((w != own) & (w != -1)))
-    return keep
+    return adaptive_seed_mask_allx({0: large_lab}, seeds)
 
 
 def subset_seeds(seeds, mask):

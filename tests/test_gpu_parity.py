@@ -18,6 +18,22 @@ from biomedisa_gb300.synthetic import plain_volume, sparse_labels
 pytestmark = pytest.mark.gpu
 
 
+def _large_allx_case():
+    """Labels on z-slices 3 and 11, y-slice 15 and x-slice 400 of a
+    16 x 22 x 460 volume (planes wider than the adaptive window), a -1 patch."""
+    lab = np.zeros((16, 22, 460), np.int32)
+    for z in (3, 11):
+        lab[z, :, :300] = 1
+        lab[z, :, 300:450] = 2
+    lab[11, 6:10, 40:70] = -1
+    lab[:, 15, :300] = 1
+    lab[:, 15, 300:420] = 2
+    lab[:, :, 400] = 2
+    lab[4:9, 5:12, 400] = 1
+    img = (np.random.default_rng(6).normal(90, 20, lab.shape) + 60 * (lab == 2)).clip(0, 255).astype(np.uint8)
+    return lab, img
+
+
 def _cases():
     img, lab, truth = plain_volume(seed=1, shape=(40, 36, 34), z_every=5, semi=(6, 12))
     base = dict(nbrw=3, sorw=70, smooth=3, uncertainty=True, return_hits=True)
@@ -70,6 +86,19 @@ def _cases():
     ll[15] = 1
     il = (np.random.default_rng(4).normal(90, 20, ll.shape) + 60 * (ll == 2)).clip(0, 255).astype(np.uint8)
     yield "large_seeding_wide", il, ll, dict(base, nbrw=2, sorw=40, smooth=2, seeding="large")
+    # the all-axis large path's seed set (every slice with a positive label on
+    # each axis, one box per axis, adaptive seeds in slice coordinates)
+    yield "large_allx_u8", img3, lab3, dict(base, allaxis=True, smooth=2, seeding="large")
+    la, ia = _large_allx_case()
+    yield "large_allx_wide", ia, la, dict(base, nbrw=2, sorw=40, allaxis=True, smooth=2, seeding="large")
+    lb2 = np.zeros(big.shape, np.int32)
+    for z in range(0, 30, 4):
+        lb2[z, 110:150, 105:145] = np.where(tb[z, 110:150, 105:145] == 1, 1, 2)
+    for y in (118, 131):
+        lb2[1:29, y, 100:150] = np.where(tb[1:29, y, 100:150] == 1, 1, 2)
+    lb2[2:28, 112:148, 126] = np.where(tb[2:28, 112:148, 126] == 1, 1, 2)
+    lb2[6:9, 120:124, 126] = -1
+    yield "large_allx_inner", big, lb2, dict(base, nbrw=1, sorw=40, allaxis=True, smooth=1, seeding="large")
 
 
 CASES = list(_cases())
@@ -236,4 +265,22 @@ def test_large_seeding_box_and_count(cuda):
     seeds = O.extract_seeds(np.pad(il, 1)[az:bz, ay:by, ax:bx], llab, [(0, k) for k in idx], O.pre_processing(
         np.pad(ll, 1))[1])
     keep = O.adaptive_seed_mask(llab, seeds)
+    assert int(job.n_seeds.item()) == int(keep.sum()) < len(keep)
+
+
+def test_large_allx_boxes_and_count(cuda):
+    """All-axis large-path seeding: the slice list, the per-axis boxes and the
+    number of seeds kept by the adaptive filter equal the oracle's."""
+    lab, img = _large_allx_case()
+    lab[3, 2:20, 290:320] = 3  # a third label inside the z-slices
+    job = _job(img, lab, allaxis=True, seeding="large")
+    lp = np.pad(lab, 1)
+    az, bz, ay, by, ax, bx = O.predict_blocksize(lp)
+    lc = np.ascontiguousarray(lp[az:bz, ay:by, ax:bx])
+    sl = O.large_allx_slice_list(lc)
+    llabs, boxes = O.large_allx_labels(lc, sl)
+    for a, box in boxes.items():
+        assert tuple(job.large_boxes[a]) == tuple(box), a
+    seeds = O.extract_seeds(np.pad(img, 1)[az:bz, ay:by, ax:bx], llabs, sl, O.pre_processing(lp)[1])
+    keep = O.adaptive_seed_mask_allx(llabs, seeds)
     assert int(job.n_seeds.item()) == int(keep.sum()) < len(keep)
