@@ -13,8 +13,8 @@ libsmartinterp.so on one GPU. Differences from the reference, by design:
     reference's literal 0.01 is binary64);
   * every volume takes the plain full walk (the reference switches to its
     seed-subsampling large path above 2e9 bytes, interpolation.py:196);
-  * file I/O, MPI ranks, Django and acwe are not part of this path; clean and
-    fill run on the device (postprocess.py).
+  * file I/O, MPI ranks and Django are not part of this path; clean, fill
+    (postprocess.py) and acwe (active_contour.py) run on the device.
 """
 from __future__ import annotations
 
@@ -695,8 +695,11 @@ def smart_interpolation(data, labelData, nbrw=10, sorw=4000, acwe=False, acwe_al
     shared-memory brick walker, uint8 only; 'packed': one thread per walk) and
     the packed walker's launch shape (``walk_grid``, ``walk_block``,
     ``walk_order``). All walkers give identical hit maps. ``seeding='large'``
-    walks the seed set of the reference's large path (slice skipping, label
-    box, adaptive seeds; z-slices only) instead of every seed.
+    walks the seed set of the reference's large path (z-slices: slice
+    skipping, label box, adaptive seeds; all-axis: every slice with a positive
+    label, a label box per axis, adaptive seeds in each slice's plane) instead
+    of every seed. ``acwe=True`` adds 'acwe' and 'refined' (the reference's
+    activeContour on the regular result, rw_small.py:246-255).
     ``rng``: the walk's random stream — 'philox' (counter-based Philox4x32-10
     keyed by ``rng_seed``, the default) or 'reference' (the reference walker's
     own binary32 MRG recurrence, seeded per seed as its CUDA kernel does,
