@@ -89,7 +89,9 @@ __global__ void __launch_bounds__(256) bucket_kernel(const uint4* __restrict__ s
                                                      const SeedRec* __restrict__ seeds, uint32_t ns, int sorw,
                                                      BrickGeom g, uint32_t* __restrict__ counts,
                                                      const uint32_t* __restrict__ offsets,
-                                                     uint4* __restrict__ states_out) {
+                                                     uint4* __restrict__ states_out,
+                                                     const uint32_t* __restrict__ n_dev = nullptr) {
+  if (n_dev) n = *n_dev;  // the count lives on the device (device-side sweep loop)
   const int lane = threadIdx.x & 31;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
@@ -379,7 +381,9 @@ template <bool kFloat>
 __global__ void __launch_bounds__(256) sweep_kernel(const void* __restrict__ packed, BrickGeom g,
                                                     uint4* __restrict__ states, uint32_t n_live, uint32_t K,
                                                     const SeedRec* __restrict__ seeds, uint32_t k0, uint32_t k1,
-                                                    uint32_t* __restrict__ hits, uint32_t* __restrict__ next_counts) {
+                                                    uint32_t* __restrict__ hits, uint32_t* __restrict__ next_counts,
+                                                    const uint32_t* __restrict__ live_dev) {
+  if (live_dev) n_live = *live_dev;  // the count lives on the device (device-side sweep loop)
   __shared__ int32_t s_delta[6];
   if (threadIdx.x < 6) {
     const int32_t F = (int32_t)g.F, X = g.Xc;
@@ -391,6 +395,15 @@ __global__ void __launch_bounds__(256) sweep_kernel(const void* __restrict__ pac
   const uint32_t stride = gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
   const uint64_t nz = f2_negzero();
+  // next sweep's bucket counts, warp-aggregated (whole warps call this)
+  auto count = [&](bool alive, const uint4& st) {
+    const uint32_t act = __ballot_sync(0xffffffffu, alive);
+    if (alive) {
+      const uint32_t key = bucket_of(g, st);
+      const uint32_t peers = __match_any_sync(act, key);
+      if (lane == __ffs(peers) - 1) atomicAdd(&next_counts[key], (uint32_t)__popc(peers));
+    }
+  };
   // warp-uniform trip count, so the counting below runs with full warps
   const uint32_t i_end = (n_live + 31u) & ~31u;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < i_end; i += stride) {
@@ -408,11 +421,78 @@ __global__ void __launch_bounds__(256) sweep_kernel(const void* __restrict__ pac
       states[i] = st;
       alive = t_end != te;
     }
-    const uint32_t act = __ballot_sync(0xffffffffu, alive);
-    if (alive) {
-      const uint32_t key = bucket_of(g, st);
-      const uint32_t peers = __match_any_sync(act, key);
-      if (lane == __ffs(peers) - 1) atomicAdd(&next_counts[key], (uint32_t)__popc(peers));
+    count(alive, st);
+  }
+}
+
+// The same sweep with N consecutive walkers per thread (walk_steps_multi);
+// kMinBlocks CTAs of kThreads per SM.
+template <bool kFloat, int N, int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+    sweep_multi_kernel(const void* __restrict__ packed, BrickGeom g, uint4* __restrict__ states, uint32_t n_live,
+                       uint32_t K, const SeedRec* __restrict__ seeds, uint32_t k0, uint32_t k1,
+                       uint32_t* __restrict__ hits, uint32_t* __restrict__ next_counts,
+                       const uint32_t* __restrict__ live_dev) {
+  if (live_dev) n_live = *live_dev;  // the count lives on the device (device-side sweep loop)
+  __shared__ int32_t s_delta[6];
+  if (threadIdx.x < 6) {
+    const int32_t F = (int32_t)g.F, X = g.Xc;
+    s_delta[threadIdx.x] = threadIdx.x == 0 ? F : threadIdx.x == 1 ? -F : threadIdx.x == 2 ? X
+                           : threadIdx.x == 3 ? -X : threadIdx.x == 4 ? 1 : -1;
+  }
+  __syncthreads();
+  const size_t V = (size_t)g.F * g.Zc;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  const uint64_t nz = f2_negzero();
+  // consecutive walkers (same bucket order: neighbours in the volume); the
+  // trip count is warp-uniform so the counting runs with full warps
+  const uint32_t n_groups = (n_live + (uint32_t)N - 1u) / (uint32_t)N;
+  const uint32_t i_end = (n_groups + 31u) & ~31u;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < i_end; i += stride) {
+    uint4 st[N];
+    bool alive[N];
+    uint32_t te[N];
+    PairWalker W[N];
+#pragma unroll
+    for (int w = 0; w < N; ++w) {
+      st[w] = make_uint4(0u, 0u, 0u, 0u);
+      alive[w] = false;
+      te[w] = 0u;
+      W[w] = pair_walker(0u, 0u, 0u, 0.0f, 0.0f, 0u, 0u, 0u, hits);  // no steps without a walker
+    }
+    if (i < n_groups) {
+#pragma unroll
+      for (int w = 0; w < N; ++w) {
+        const uint32_t idx = (uint32_t)N * i + (uint32_t)w;
+        if (idx < n_live) {
+          st[w] = states[idx];
+          const SeedRec sd = seeds[st[w].y];
+          te[w] = st[w].w & 0xFFFFFFu;
+          W[w] = pair_walker(st[w].x, st[w].z, min(st[w].z + K, te[w]), sd.c, sd.b, sd.pos, seed_axis(sd.meta),
+                             seed_label(sd.meta), hits + (size_t)(st[w].w >> 24) * V);
+        }
+      }
+      walk_steps_multi<kFloat, N>(packed, W, k0, k1, s_delta, nz);
+#pragma unroll
+      for (int w = 0; w < N; ++w) {
+        const uint32_t idx = (uint32_t)N * i + (uint32_t)w;
+        if (idx < n_live) {
+          st[w].x = W[w].pos;
+          st[w].z = W[w].t_end;
+          states[idx] = st[w];
+          alive[w] = W[w].t_end != te[w];
+        }
+      }
+    }
+#pragma unroll
+    for (int w = 0; w < N; ++w) {
+      const uint32_t act = __ballot_sync(0xffffffffu, alive[w]);
+      if (alive[w]) {
+        const uint32_t key = bucket_of(g, st[w]);
+        const uint32_t peers = __match_any_sync(act, key);
+        if (lane == __ffs(peers) - 1) atomicAdd(&next_counts[key], (uint32_t)__popc(peers));
+      }
     }
   }
 }
@@ -604,6 +684,85 @@ namespace {
 constexpr uint64_t kBatchWalks = 1ull << 25;  // default walks per seed range of si_walk_sorted
 constexpr int kSortEdge = 6;
 std::atomic<unsigned long long> g_range_walks{0};  // 0 = kBatchWalks (si_walk_sorted_set_range)
+std::atomic<int> g_sweep_pairs{1};  // sweep kernel mode (si_walk_sorted_set_pairs)
+std::atomic<int> g_device_loop{1};  // 1: device-side sweep loop (si_walk_sorted_set_loop)
+std::atomic<unsigned long long> g_round_limit{0};  // 0 = kRoundLimit (si_walk_sorted_set_round_limit)
+constexpr uint64_t kRoundLimit = 1ull << 24;
+constexpr int kCtrWords = 8;
+
+uint32_t round_limit() {
+  const unsigned long long v = g_round_limit.load(std::memory_order_relaxed);
+  return (uint32_t)std::min<uint64_t>(v ? v : kRoundLimit, 0xFFFFFFFFull);
+}
+
+// After a sweep: the states the next scatter reads are the ones this sweep
+// advanced (ctrs[0] of the scan before it); ctrs[4] counts sweeps that ran.
+__global__ void round_shift_kernel(uint32_t* __restrict__ ctrs) {
+  const uint32_t live = ctrs[0];
+  ctrs[3] = live;
+  if (live) ctrs[4] += 1u;
+}
+
+// End of a loop iteration: continue while walkers are live and fewer than
+// `limit` sweeps ran; reaching the limit with live walkers sets ctrs[5].
+__global__ void round_cond_kernel(uint32_t* __restrict__ ctrs, cudaGraphConditionalHandle h, uint32_t limit) {
+  const uint32_t live = ctrs[0];
+  const bool over = live != 0u && ctrs[4] >= limit;
+  if (over) ctrs[5] = 1u;
+  cudaGraphSetConditional(h, (live != 0u && !over) ? 1u : 0u);
+}
+
+// A stream of this device for capturing loop bodies (never executes work).
+cudaStream_t capture_stream() {
+  static std::mutex mu;
+  static cudaStream_t streams[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!streams[dev] && cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking) != cudaSuccess)
+    streams[dev] = nullptr;
+  return streams[dev];
+}
+
+// An executable graph holding one WHILE node whose body is what enqueue(s, h)
+// puts on stream s (recorded by stream capture). The condition starts at 1
+// on every launch; a kernel of the body sets it with cudaGraphSetConditional.
+template <class F>
+int build_while_graph(F&& enqueue, cudaGraphExec_t* exec) {
+  cudaStream_t cs = capture_stream();
+  if (!cs) return set_error(SI_ERR_CUDA, "si_walk_sorted: no capture stream");
+  cudaGraph_t graph = nullptr;
+  if (cudaGraphCreate(&graph, 0) != cudaSuccess) return set_error(SI_ERR_CUDA, "si_walk_sorted: graph create");
+  int rc = SI_OK;
+  cudaGraphConditionalHandle h;
+  cudaGraphNodeParams cp = {};
+  cudaGraphNode_t node;
+  if (cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+    rc = set_error(SI_ERR_CUDA, "si_walk_sorted: conditional handle: %s", cudaGetErrorString(cudaGetLastError()));
+  } else {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    if (cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp) != cudaSuccess)
+      rc = set_error(SI_ERR_CUDA, "si_walk_sorted: while node: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  if (rc == SI_OK) {
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if (cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+      rc = set_error(SI_ERR_CUDA, "si_walk_sorted: capture: %s", cudaGetErrorString(cudaGetLastError()));
+    } else {
+      enqueue(cs, h);
+      cudaGraph_t captured = nullptr;
+      if (cudaStreamEndCapture(cs, &captured) != cudaSuccess)
+        rc = set_error(SI_ERR_CUDA, "si_walk_sorted: capture end: %s", cudaGetErrorString(cudaGetLastError()));
+      else if (cudaGraphInstantiate(exec, graph, 0) != cudaSuccess)
+        rc = set_error(SI_ERR_CUDA, "si_walk_sorted: instantiate: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+  }
+  cudaGraphDestroy(graph);
+  return rc;
+}
 
 uint64_t range_walks() {
   const unsigned long long v = g_range_walks.load(std::memory_order_relaxed);
@@ -632,7 +791,7 @@ SortLayout sort_layout(const BrickGeom& g, uint64_t max_walks, int nol) {
   L.sums = off;
   off = align_up(off + (nblocks + 1) * sizeof(uint32_t), 256);
   L.ctrs = off;
-  off = align_up(off + 4 * sizeof(uint32_t), 256);
+  off = align_up(off + kCtrWords * sizeof(uint32_t), 256);
   L.total = off;
   return L;
 }
@@ -651,6 +810,26 @@ extern "C" int si_walk_sorted_scratch(int Zc, int Yc, int Xc, uint64_t max_walks
 extern "C" int si_walk_sorted_set_range(unsigned long long walks_per_range) {
   clear_error();
   g_range_walks.store(walks_per_range, std::memory_order_relaxed);
+  return SI_OK;
+}
+
+extern "C" int si_walk_sorted_set_pairs(int pairs) {
+  clear_error();
+  if (pairs < 0 || pairs > 3) return set_error(SI_ERR_ARG, "si_walk_sorted_set_pairs: 0 to 3");
+  g_sweep_pairs.store(pairs, std::memory_order_relaxed);
+  return SI_OK;
+}
+
+extern "C" int si_walk_sorted_set_loop(int device_loop) {
+  clear_error();
+  if (device_loop < 0 || device_loop > 1) return set_error(SI_ERR_ARG, "si_walk_sorted_set_loop: 0 or 1");
+  g_device_loop.store(device_loop, std::memory_order_relaxed);
+  return SI_OK;
+}
+
+extern "C" int si_walk_sorted_set_round_limit(unsigned long long sweeps) {
+  clear_error();
+  g_round_limit.store(sweeps, std::memory_order_relaxed);
   return SI_OK;
 }
 
@@ -705,6 +884,108 @@ extern "C" int si_walk_sorted(const void* packed, int work_is_float, int Zc, int
   // does not depend on the ranges.
   const uint64_t per_range = range_walks();
   const uint64_t nbatch = std::max<uint64_t>(1, (walks + per_range / 2) / per_range);
+  // walkers per thread: mode 0 -> 1, 1 -> 2, 2 -> 3, 3 -> 4
+  const int mode = g_sweep_pairs.load(std::memory_order_relaxed);
+  const int tpb = mode == 3 ? 128 : 256;
+  const uint64_t cap = (uint64_t)sms * (tpb == 128 ? 16 : 8);
+  // one sweep launch over states s_in (live count live_now, or *live_dev when
+  // the count stays on the device) into the next round's bucket sizes c_next
+  auto sweep = [&](cudaStream_t s, uint4* s_in, uint32_t live_now, const uint32_t* live_dev,
+                   const SeedRec* sd, uint32_t* c_next) {
+    const uint64_t per = (uint64_t)mode + 1;
+    const uint64_t threads = live_dev ? cap * tpb : ((uint64_t)live_now + per - 1) / per;
+    const uint64_t want_blocks = (threads + tpb - 1) / tpb;
+    const uint32_t blocks = (uint32_t)(want_blocks < cap ? want_blocks : cap);
+#define SI_SWEEP(KERNEL) KERNEL<<<blocks, tpb, 0, s>>>(packed, g, s_in, live_now, (uint32_t)sweep_steps, sd, k0, k1, \
+                                                       hits, c_next, live_dev)
+#define SI_SWEEPS(F)                                   \
+  do {                                                 \
+    if (mode == 3)                                     \
+      SI_SWEEP((sweep_multi_kernel<F, 4, 128, 3>));    \
+    else if (mode == 2)                                \
+      SI_SWEEP((sweep_multi_kernel<F, 3, 256, 2>));    \
+    else if (mode == 1)                                \
+      SI_SWEEP((sweep_multi_kernel<F, 2, 256, 3>));    \
+    else                                               \
+      SI_SWEEP(sweep_kernel<F>);                       \
+  } while (0)
+    if (work_is_float)
+      SI_SWEEPS(true);
+    else
+      SI_SWEEPS(false);
+#undef SI_SWEEPS
+#undef SI_SWEEP
+  };
+  auto scan = [&](cudaStream_t s, const uint32_t* c) {
+    scan_sums_kernel<<<nblocks, 256, 0, s>>>(c, nbt, sums);
+    scan_top_kernel<<<1, 1024, 0, s>>>(sums, nblocks);
+    scan_apply_kernel<<<nblocks, 256, 0, s>>>(c, nbt, sums, offsets, ctrs);
+  };
+  if (g_device_loop.load(std::memory_order_relaxed)) {
+    // Device-side sweep loop: no host round trip per sweep. ctrs: [0] live
+    // walkers after the last scan, [3] the states the next scatter reads,
+    // [4] sweeps run, [5] round limit hit.
+    const uint32_t limit = round_limit();
+    if (cudaMemsetAsync(ctrs, 0, kCtrWords * sizeof(uint32_t), st) != cudaSuccess)
+      return set_error(SI_ERR_CUDA, "si_walk_sorted: memset failed");
+    std::vector<cudaGraphExec_t> execs;
+    int rc = SI_OK;
+    uint32_t* C0 = counts;
+    uint32_t* C1 = counts2;
+    for (uint64_t bidx = 0; bidx < nbatch && rc == SI_OK; ++bidx) {
+      const uint32_t sa = (uint32_t)((uint64_t)ns * bidx / nbatch), se = (uint32_t)((uint64_t)ns * (bidx + 1) / nbatch);
+      if (se == sa) continue;
+      const SeedRec* sd = sd_all + sa;
+      const uint32_t ns_b = se - sa;
+      const uint64_t n0 = (uint64_t)ns_b * (uint64_t)nbrw;
+      // round 0 from the virtual (seed, walk) pairs into states[0]
+      cudaMemsetAsync(C0, 0, count_bytes, st);
+      bucket_kernel<true, false><<<gb, 256, 0, st>>>(nullptr, n0, sd, ns_b, sorw, g, C0, nullptr, nullptr);
+      scan(st, C0);
+      cudaMemsetAsync(C0, 0, count_bytes, st);
+      cudaMemsetAsync(C1, 0, count_bytes, st);
+      bucket_kernel<true, true><<<gb, 256, 0, st>>>(nullptr, n0, sd, ns_b, sorw, g, C0, offsets, states[0]);
+      sweep(st, states[0], 0u, ctrs, sd, C1);
+      round_shift_kernel<<<1, 1, 0, st>>>(ctrs);
+      scan(st, C1);
+      rc = check_launch("si_walk_sorted: round 0");
+      if (rc) break;
+      // later rounds: two per loop iteration (states[0] -> states[1] with
+      // counts C1 -> C0, then back), while walkers are live
+      cudaGraphExec_t exec = nullptr;
+      rc = build_while_graph(
+          [&](cudaStream_t cs, cudaGraphConditionalHandle h) {
+            for (int half = 0; half < 2; ++half) {
+              uint32_t* cur_c = half ? C0 : C1;  // scanned sizes -> scatter cursor
+              uint32_t* nxt_c = half ? C1 : C0;  // the sweep's counts of the round after
+              uint4* s_in = states[half];
+              uint4* s_out = states[1 - half];
+              cudaMemsetAsync(cur_c, 0, count_bytes, cs);
+              cudaMemsetAsync(nxt_c, 0, count_bytes, cs);
+              bucket_kernel<false, true><<<gb, 256, 0, cs>>>(s_in, 0, sd, ns_b, sorw, g, cur_c, offsets, s_out,
+                                                             ctrs + 3);
+              sweep(cs, s_out, 0u, ctrs, sd, nxt_c);
+              round_shift_kernel<<<1, 1, 0, cs>>>(ctrs);
+              scan(cs, nxt_c);
+            }
+            round_cond_kernel<<<1, 1, 0, cs>>>(ctrs, h, limit);
+          },
+          &exec);
+      if (rc) break;
+      execs.push_back(exec);
+      if (cudaGraphLaunch(exec, st) != cudaSuccess) rc = set_error(SI_ERR_CUDA, "si_walk_sorted: graph launch failed");
+    }
+    uint32_t host_ctrs[kCtrWords] = {};
+    if (cudaMemcpyAsync(host_ctrs, ctrs, sizeof(host_ctrs), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      rc = rc ? rc : set_error(SI_ERR_CUDA, "si_walk_sorted: %s", cudaGetErrorString(cudaGetLastError()));
+    for (cudaGraphExec_t e : execs) cudaGraphExecDestroy(e);
+    if (rc) return rc;
+    if (host_ctrs[5]) return set_error(SI_ERR_LIMIT, "si_walk_sorted: no convergence within %u sweeps", limit);
+    if (rounds_out) *rounds_out = (int)host_ctrs[4];
+    return check_launch("si_walk_sorted");
+  }
+  // Host-side sweep loop: the live count is read back after every scan.
   int rounds = 0;
   for (uint64_t bidx = 0; bidx < nbatch; ++bidx) {
     const uint32_t sa = (uint32_t)((uint64_t)ns * bidx / nbatch), se = (uint32_t)((uint64_t)ns * (bidx + 1) / nbatch);
@@ -720,14 +1001,13 @@ extern "C" int si_walk_sorted(const void* packed, int work_is_float, int Zc, int
     bucket_kernel<true, false><<<gb, 256, 0, st>>>(nullptr, n_prev, sd, ns_b, sorw, g, counts, nullptr, nullptr);
     for (int batch_rounds = 0;; ++batch_rounds, ++rounds) {
       const bool first = batch_rounds == 0;
-      scan_sums_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums);
-      scan_top_kernel<<<1, 1024, 0, st>>>(sums, nblocks);
-      scan_apply_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums, offsets, ctrs);
+      scan(st, counts);
       uint32_t live_now = 0;
       if (cudaMemcpyAsync(&live_now, ctrs, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
           cudaStreamSynchronize(st) != cudaSuccess)
         return set_error(SI_ERR_CUDA, "si_walk_sorted: round %d: %s", rounds, cudaGetErrorString(cudaGetLastError()));
       if (live_now == 0) break;
+      if ((uint64_t)rounds >= round_limit()) return set_error(SI_ERR_LIMIT, "si_walk_sorted: no convergence");
       // counts becomes the scatter's per-bucket cursor, counts2 the next round's sizes
       if (cudaMemsetAsync(counts, 0, count_bytes, st) != cudaSuccess ||
           cudaMemsetAsync(counts2, 0, count_bytes, st) != cudaSuccess)
@@ -740,19 +1020,11 @@ extern "C" int si_walk_sorted(const void* packed, int work_is_float, int Zc, int
         bucket_kernel<false, true><<<gb, 256, 0, st>>>(states[cur], n_prev, sd, ns_b, sorw, g, counts, offsets,
                                                        states[nxt]);
       cur = nxt;
-      const uint64_t want_blocks = ((uint64_t)live_now + 255) / 256;
-      const uint32_t blocks = (uint32_t)(want_blocks < (uint64_t)sms * 8 ? want_blocks : (uint64_t)sms * 8);
-      if (work_is_float)
-        sweep_kernel<true><<<blocks, 256, 0, st>>>(packed, g, states[cur], live_now, (uint32_t)sweep_steps, sd, k0,
-                                                   k1, hits, counts2);
-      else
-        sweep_kernel<false><<<blocks, 256, 0, st>>>(packed, g, states[cur], live_now, (uint32_t)sweep_steps, sd, k0,
-                                                    k1, hits, counts2);
+      sweep(st, states[cur], live_now, nullptr, sd, counts2);
       const int rc = check_launch("si_walk_sorted: sweep");
       if (rc) return rc;
       std::swap(counts, counts2);
       n_prev = live_now;
-      if (batch_rounds > (1 << 24)) return set_error(SI_ERR_LIMIT, "si_walk_sorted: no convergence");
     }
   }
   if (rounds_out) *rounds_out = rounds;
@@ -849,36 +1121,100 @@ __global__ void __launch_bounds__(256) bbucket_kernel(const uint4* __restrict__ 
   }
 }
 
-__global__ void __launch_bounds__(256) bsweep_kernel(const VolDesc* __restrict__ vols, int n_vols,
-                                                     uint4* __restrict__ states, uint32_t n_live, uint32_t K,
-                                                     uint32_t k0, uint32_t k1) {
+// One sweep of the batched walkers. kPair: a thread takes two consecutive
+// walkers and advances them together (walk_steps_multi) when they belong to
+// the same volume, else one after the other. The next sweep's bucket counts
+// are formed here (warp-aggregated atomics into next_counts).
+template <bool kPair, int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) bsweep_kernel(const VolDesc* __restrict__ vols_g, int n_vols,
+                                                                 uint4* __restrict__ states, uint32_t n_live,
+                                                                 uint32_t K, uint32_t k0, uint32_t k1, int edge,
+                                                                 uint32_t* __restrict__ next_counts) {
   __shared__ int32_t s_delta[256 * 6];  // move offsets of every volume
+  __shared__ VolDesc vols[256];         // the volume table (at most 256 volumes)
+  for (int i = threadIdx.x; i < n_vols; i += blockDim.x) vols[i] = vols_g[i];
   for (int i = threadIdx.x; i < n_vols * 6; i += blockDim.x) {
-    const VolDesc& d = vols[i / 6];
+    const VolDesc& d = vols_g[i / 6];
     const int dir = i % 6;
     const int32_t mag = dir < 2 ? (int32_t)d.F : (dir < 4 ? d.Xc : 1);
     s_delta[i] = (dir & 1) ? -mag : mag;
   }
   __syncthreads();
   const uint32_t stride = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
   const uint64_t nz = f2_negzero();
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_live; i += stride) {
-    uint4 st = states[i];
-    const uint32_t v = bvol(st);
-    const VolDesc& d = vols[v];
-    const SeedRec sd = d.seeds[st.y];
-    const uint32_t t = bstep(st);
-    const uint32_t te = st.w & 0xFFFFFFu;
-    const uint32_t t_end = min(t + K, te);
-    uint32_t* __restrict__ hl = d.hits + (size_t)(st.w >> 24) * ((size_t)d.F * d.Zc);
-    if (d.is_float)
-      st.x = walk_steps<true>(d.packed, st.x, t, t_end, sd.c, sd.b, sd.pos, seed_axis(sd.meta), seed_label(sd.meta),
-                              k0, k1, hl, s_delta + 6 * v, nz);
-    else
-      st.x = walk_steps<false>(d.packed, st.x, t, t_end, sd.c, sd.b, sd.pos, seed_axis(sd.meta),
-                               seed_label(sd.meta), k0, k1, hl, s_delta + 6 * v, nz);
-    st.z = t_end | (st.z & 0xFF000000u);
-    states[i] = st;
+  constexpr uint32_t N = kPair ? 2u : 1u;
+  const uint32_t n_groups = (n_live + N - 1u) / N;
+  const uint32_t i_end = (n_groups + 31u) & ~31u;  // warp-uniform: the counting runs with full warps
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < i_end; i += stride) {
+    uint4 st[N];
+    bool alive[N];
+#pragma unroll
+    for (uint32_t w = 0; w < N; ++w) {
+      st[w] = make_uint4(0u, 0u, 0u, 0u);
+      alive[w] = false;
+    }
+    if (i < n_groups) {
+      PairWalker W[N];
+      uint32_t te[N], vol[N];
+      bool has[N];
+#pragma unroll
+      for (uint32_t w = 0; w < N; ++w) {
+        const uint32_t idx = N * i + w;
+        has[w] = idx < n_live;
+        te[w] = 0u;
+        vol[w] = 0u;
+        W[w] = pair_walker(0u, 0u, 0u, 0.0f, 0.0f, 0u, 0u, 0u, nullptr);
+        if (has[w]) {
+          st[w] = states[idx];
+          vol[w] = bvol(st[w]);
+          const VolDesc& d = vols[vol[w]];
+          const SeedRec sd = d.seeds[st[w].y];
+          const uint32_t t = bstep(st[w]);
+          te[w] = st[w].w & 0xFFFFFFu;
+          W[w] = pair_walker(st[w].x, t, min(t + K, te[w]), sd.c, sd.b, sd.pos, seed_axis(sd.meta),
+                             seed_label(sd.meta), d.hits + (size_t)(st[w].w >> 24) * ((size_t)d.F * d.Zc));
+        }
+      }
+      const VolDesc& d0 = vols[vol[0]];
+      const int32_t* sdl0 = s_delta + 6 * vol[0];
+      if (kPair && has[N - 1] && vol[N - 1] == vol[0]) {
+        if (d0.is_float)
+          walk_steps_multi<true, N>(d0.packed, W, k0, k1, sdl0, nz);
+        else
+          walk_steps_multi<false, N>(d0.packed, W, k0, k1, sdl0, nz);
+      } else {
+#pragma unroll
+        for (uint32_t w = 0; w < N; ++w) {
+          if (!has[w]) continue;
+          const VolDesc& d = vols[vol[w]];
+          PairWalker& A = W[w];
+          if (d.is_float)
+            A.pos = walk_steps<true>(d.packed, A.pos, A.t, A.t_end, A.c, A.bf, A.seed_pos, A.axis, A.label, k0, k1,
+                                     A.hl, s_delta + 6 * vol[w], nz);
+          else
+            A.pos = walk_steps<false>(d.packed, A.pos, A.t, A.t_end, A.c, A.bf, A.seed_pos, A.axis, A.label, k0, k1,
+                                      A.hl, s_delta + 6 * vol[w], nz);
+        }
+      }
+#pragma unroll
+      for (uint32_t w = 0; w < N; ++w) {
+        if (!has[w]) continue;
+        st[w].x = W[w].pos;
+        st[w].z = W[w].t_end | (st[w].z & 0xFF000000u);
+        states[N * i + w] = st[w];
+        alive[w] = W[w].t_end != te[w];
+      }
+    }
+#pragma unroll
+    for (uint32_t w = 0; w < N; ++w) {
+      const uint32_t act = __ballot_sync(0xffffffffu, alive[w]);
+      if (alive[w]) {
+        const uint32_t key = bbucket(vols[bvol(st[w])], edge, st[w]);
+        const uint32_t peers = __match_any_sync(act, key);
+        if (lane == __ffs(peers) - 1) atomicAdd(&next_counts[key], (uint32_t)__popc(peers));
+      }
+    }
   }
 }
 
@@ -891,8 +1227,8 @@ struct BatchPlan {
   std::vector<si::VolDesc> vols;
   uint64_t walks = 0;
   uint32_t nbt = 0;
-  size_t off_vols = 0, off_states0 = 0, off_states1 = 0, off_counts = 0, off_offsets = 0, off_sums = 0,
-         off_ctrs = 0, total = 0;
+  size_t off_vols = 0, off_states0 = 0, off_states1 = 0, off_counts = 0, off_counts2 = 0, off_offsets = 0,
+         off_sums = 0, off_ctrs = 0, total = 0;
 };
 
 int make_batch_plan(const si_volume_t* vols, int n_vols, int nbrw, int edge, const uint32_t* ns_host,
@@ -938,6 +1274,8 @@ int make_batch_plan(const si_volume_t* vols, int n_vols, int nbrw, int edge, con
   P.off_states1 = off;
   off = si::align_up(off + P.walks * sizeof(uint4), 256);
   P.off_counts = off;
+  off = si::align_up(off + ((size_t)P.nbt + 1) * sizeof(uint32_t), 256);
+  P.off_counts2 = off;
   off = si::align_up(off + ((size_t)P.nbt + 1) * sizeof(uint32_t), 256);
   P.off_offsets = off;
   off = si::align_up(off + ((size_t)P.nbt + 1) * sizeof(uint32_t), 256);
@@ -1010,16 +1348,18 @@ extern "C" int si_walk_sorted_batch(const si_volume_t* vols, int n_vols, int nbr
   const uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
   int cur = 0, rounds = 0;
   uint64_t n_prev = P.walks;
+  uint32_t* counts2 = reinterpret_cast<uint32_t*>(base + Pmax.off_counts2);
+  const size_t count_bytes = (size_t)(nbt + 1) * sizeof(uint32_t);
+  // round 0's bucket sizes come from a counting pass over the virtual
+  // (volume, seed, walk) triples; every later round's from the previous sweep
+  if (cudaMemsetAsync(counts, 0, count_bytes, st) != cudaSuccess)
+    return set_error(SI_ERR_CUDA, "si_walk_sorted_batch: memset failed");
+  bbucket_kernel<true, false><<<gb, 256, 0, st>>>(nullptr, n_prev, d_vols, n_vols, sorw, sort_edge, counts, nullptr,
+                                                  nullptr);
+  // walker pairs unless mode 0
+  const bool pairs = g_sweep_pairs.load(std::memory_order_relaxed) != 0;
   for (;; ++rounds) {
     const bool first = rounds == 0;
-    if (cudaMemsetAsync(counts, 0, (size_t)(nbt + 1) * sizeof(uint32_t), st) != cudaSuccess)
-      return set_error(SI_ERR_CUDA, "si_walk_sorted_batch: memset failed");
-    if (first)
-      bbucket_kernel<true, false><<<gb, 256, 0, st>>>(nullptr, n_prev, d_vols, n_vols, sorw, sort_edge, counts,
-                                                      nullptr, nullptr);
-    else
-      bbucket_kernel<false, false><<<gb, 256, 0, st>>>(states[cur], n_prev, d_vols, n_vols, sorw, sort_edge, counts,
-                                                       nullptr, nullptr);
     scan_sums_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums);
     scan_top_kernel<<<1, 1024, 0, st>>>(sums, nblocks);
     scan_apply_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums, offsets, ctrs);
@@ -1029,7 +1369,9 @@ extern "C" int si_walk_sorted_batch(const si_volume_t* vols, int n_vols, int nbr
       return set_error(SI_ERR_CUDA, "si_walk_sorted_batch: round %d: %s", rounds,
                        cudaGetErrorString(cudaGetLastError()));
     if (live_now == 0) break;
-    if (cudaMemsetAsync(counts, 0, (size_t)(nbt + 1) * sizeof(uint32_t), st) != cudaSuccess)
+    // counts becomes the scatter's per-bucket cursor, counts2 the next round's sizes
+    if (cudaMemsetAsync(counts, 0, count_bytes, st) != cudaSuccess ||
+        cudaMemsetAsync(counts2, 0, count_bytes, st) != cudaSuccess)
       return set_error(SI_ERR_CUDA, "si_walk_sorted_batch: memset failed");
     const int nxt = first ? 0 : 1 - cur;
     if (first)
@@ -1039,11 +1381,20 @@ extern "C" int si_walk_sorted_batch(const si_volume_t* vols, int n_vols, int nbr
       bbucket_kernel<false, true><<<gb, 256, 0, st>>>(states[cur], n_prev, d_vols, n_vols, sorw, sort_edge, counts,
                                                       offsets, states[nxt]);
     cur = nxt;
-    const uint64_t want_blocks = ((uint64_t)live_now + 255) / 256;
+    const uint64_t threads = pairs ? ((uint64_t)live_now + 1) / 2 : (uint64_t)live_now;
+    const uint64_t want_blocks = (threads + 255) / 256;
     const uint32_t blocks = (uint32_t)(want_blocks < (uint64_t)sms * 8 ? want_blocks : (uint64_t)sms * 8);
-    bsweep_kernel<<<blocks, 256, 0, st>>>(d_vols, n_vols, states[cur], live_now, (uint32_t)sweep_steps, k0, k1);
+#define SI_BSWEEP(P, B)                                                                                         \
+  bsweep_kernel<P, B><<<blocks, 256, 0, st>>>(d_vols, n_vols, states[cur], live_now, (uint32_t)sweep_steps, k0, k1, \
+                                              sort_edge, counts2)
+    if (pairs)
+      SI_BSWEEP(true, 2);  // measured: 2 CTAs of 256 per SM (no spills) beat 3
+    else
+      SI_BSWEEP(false, 5);
+#undef SI_BSWEEP
     rc = check_launch("si_walk_sorted_batch: sweep");
     if (rc) return rc;
+    std::swap(counts, counts2);
     n_prev = live_now;
     if (rounds > (1 << 24)) return set_error(SI_ERR_LIMIT, "si_walk_sorted_batch: no convergence");
   }

@@ -231,27 +231,51 @@ __device__ __forceinline__ float byte_plus_2p23(uint32_t w, uint32_t k) {
   return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + k));
 }
 
-// One step with the uniform variate u in [0, 1) given.
+// A voxel's packed neighbourhood record: 8 bytes for uint8 volumes, 32 for
+// float volumes (see si_walk.cu).
 template <bool kFloat>
-__device__ __forceinline__ uint32_t walk_step_u(const void* __restrict__ packed_v, uint32_t pos, float u, float c,
-                                                float bf, float b23, uint32_t* __restrict__ hl,
-                                                const int32_t* s_delta, uint64_t nz) {
+struct WalkRec;
+template <>
+struct WalkRec<false> {
+  uint2 r;
+};
+template <>
+struct WalkRec<true> {
+  float4 a, b;
+};
+
+template <bool kFloat>
+__device__ __forceinline__ WalkRec<kFloat> load_rec(const void* __restrict__ packed_v, uint32_t pos);
+template <>
+__device__ __forceinline__ WalkRec<false> load_rec<false>(const void* __restrict__ packed_v, uint32_t pos) {
+  return WalkRec<false>{static_cast<const uint2*>(packed_v)[pos]};
+}
+template <>
+__device__ __forceinline__ WalkRec<true> load_rec<true>(const void* __restrict__ packed_v, uint32_t pos) {
+  const float4* rec = static_cast<const float4*>(packed_v) + 2 * (size_t)pos;
+  return WalkRec<true>{rec[0], rec[1]};
+}
+
+// One step from voxel pos, whose record is rec, with the uniform variate u in
+// [0, 1) given.
+template <bool kFloat>
+__device__ __forceinline__ uint32_t step_from_rec(const WalkRec<kFloat>& rec, uint32_t pos, float u, float c,
+                                                  float bf, float b23, uint32_t* __restrict__ hl,
+                                                  const int32_t* s_delta, uint64_t nz) {
   float w0, w1, w2, w3, w4, w5;
   uint32_t mask;
   // The (B - I) differences are formed pairwise (+z,-z), (+y,-y), (+x,-x) and
   // weighted on the packed pipe; d = B - I is exact in both record kinds
   // (uint8: (2^23 + B) - (2^23 + I); float: one RN subtraction, as before).
   const uint64_t cc = f2_splat(c);
-  if (kFloat) {
-    const float4* rec = static_cast<const float4*>(packed_v) + 2 * (size_t)pos;
-    const float4 a = rec[0], b = rec[1];
+  if constexpr (kFloat) {
     const uint64_t bf2 = f2_splat(bf);
-    edge_weight_pair(f2_sub(bf2, f2_pack(a.x, a.y)), cc, nz, w0, w1);
-    edge_weight_pair(f2_sub(bf2, f2_pack(a.z, a.w)), cc, nz, w2, w3);
-    edge_weight_pair(f2_sub(bf2, f2_pack(b.x, b.y)), cc, nz, w4, w5);
-    mask = __float_as_uint(b.z);
+    edge_weight_pair(f2_sub(bf2, f2_pack(rec.a.x, rec.a.y)), cc, nz, w0, w1);
+    edge_weight_pair(f2_sub(bf2, f2_pack(rec.a.z, rec.a.w)), cc, nz, w2, w3);
+    edge_weight_pair(f2_sub(bf2, f2_pack(rec.b.x, rec.b.y)), cc, nz, w4, w5);
+    mask = __float_as_uint(rec.b.z);
   } else {
-    const uint2 r = static_cast<const uint2*>(packed_v)[pos];
+    const uint2 r = rec.r;
     const uint64_t b2 = f2_splat(b23);
     edge_weight_pair(f2_sub(b2, f2_pack(byte_plus_2p23(r.x, 0), byte_plus_2p23(r.x, 1))), cc, nz, w0, w1);
     edge_weight_pair(f2_sub(b2, f2_pack(byte_plus_2p23(r.x, 2), byte_plus_2p23(r.x, 3))), cc, nz, w2, w3);
@@ -271,6 +295,14 @@ __device__ __forceinline__ uint32_t walk_step_u(const void* __restrict__ packed_
     atomicAdd(&hl[pos], 1u);
   }
   return pos;
+}
+
+// One step with the uniform variate u in [0, 1) given.
+template <bool kFloat>
+__device__ __forceinline__ uint32_t walk_step_u(const void* __restrict__ packed_v, uint32_t pos, float u, float c,
+                                                float bf, float b23, uint32_t* __restrict__ hl,
+                                                const int32_t* s_delta, uint64_t nz) {
+  return step_from_rec<kFloat>(load_rec<kFloat>(packed_v, pos), pos, u, c, bf, b23, hl, s_delta, nz);
 }
 
 // One step with u taken from the top 24 bits of a Philox word.
@@ -312,6 +344,61 @@ __device__ __forceinline__ uint32_t walk_steps(const void* __restrict__ packed_v
       pos = walk_step<kFloat>(packed_v, pos, philox_word(rr, t & 3u), c, bf, b23, hl, s_delta, nz);
   }
   return pos;
+}
+
+// One walker of a group advanced together (walk_steps_multi).
+struct PairWalker {
+  uint32_t pos, t, t_end;
+  float c, bf, b23;
+  uint32_t seed_pos, axis, label;
+  uint32_t* hl;
+};
+
+__device__ __forceinline__ PairWalker pair_walker(uint32_t pos, uint32_t t, uint32_t t_end, float c, float bf,
+                                                  uint32_t seed_pos, uint32_t axis, uint32_t label, uint32_t* hl) {
+  return PairWalker{pos, t, t_end, c, bf, __fadd_rn(bf, 8388608.0f), seed_pos, axis, label, hl};
+}
+
+// N walkers advanced together: while all are on aligned blocks of four
+// steps, each step issues the N record loads before any weight evaluation,
+// so one thread keeps N dependent gathers in flight. Every walker takes the
+// same steps, words and hits as walk_steps alone (each walker's own step
+// order is unchanged; hits are commutative counts).
+template <bool kFloat, int N>
+__device__ __forceinline__ void walk_steps_multi(const void* __restrict__ packed_v, PairWalker (&W)[N], uint32_t k0,
+                                                 uint32_t k1, const int32_t* s_delta, uint64_t nz) {
+  uint32_t any_t = 0u, n = 0xFFFFFFFFu;
+#pragma unroll
+  for (int w = 0; w < N; ++w) {
+    any_t |= W[w].t;
+    n = min(n, W[w].t_end - W[w].t);
+  }
+  if ((any_t & 3u) == 0u) {
+    n &= ~3u;
+    for (uint32_t k = 0; k < n; k += 4u) {
+      U4 r[N];
+#pragma unroll
+      for (int w = 0; w < N; ++w) r[w] = philox4x32_10(U4{W[w].t >> 2, W[w].seed_pos, W[w].axis, W[w].label}, k0, k1);
+#pragma unroll
+      for (uint32_t j = 0; j < 4u; ++j) {
+        WalkRec<kFloat> q[N];
+#pragma unroll
+        for (int w = 0; w < N; ++w) q[w] = load_rec<kFloat>(packed_v, W[w].pos);
+#pragma unroll
+        for (int w = 0; w < N; ++w)
+          W[w].pos = step_from_rec<kFloat>(q[w], W[w].pos, u01_from_bits(philox_word(r[w], j)), W[w].c, W[w].bf,
+                                           W[w].b23, W[w].hl, s_delta, nz);
+      }
+#pragma unroll
+      for (int w = 0; w < N; ++w) W[w].t += 4u;
+    }
+  }
+#pragma unroll
+  for (int w = 0; w < N; ++w) {
+    W[w].pos = walk_steps<kFloat>(packed_v, W[w].pos, W[w].t, W[w].t_end, W[w].c, W[w].bf, W[w].seed_pos, W[w].axis,
+                                  W[w].label, k0, k1, W[w].hl, s_delta, nz);
+    W[w].t = W[w].t_end;
+  }
 }
 
 }  // namespace si

@@ -458,7 +458,9 @@ class DeviceJob:
             self.rounds = walk_sorted(self.packed, self.work_is_float, cp.Zc, cp.Yc, cp.Xc, self.seeds,
                                       self.n_seeds, self.seed_capacity, self.nbrw, self.sorw, self.rng_seed,
                                       self.hits, nol, self.sweep_steps, self.sort_edge)
-            self.launches += 6 * self.rounds + 4
+            # per sweep: scatter, sweep, round shift and three scan kernels
+            # (+ one loop-condition kernel per two sweeps on the device loop)
+            self.launches += 6 * self.rounds + (self.rounds + 1) // 2 + 10
             return
         nat.call("si_walk", _ptr(self.packed), int(self.work_is_float), cp.Zc, cp.Yc, cp.Xc, _ptr(self.seeds),
                  _ptr(self.n_seeds), self.seed_capacity, self.nbrw, self.sorw, self.rng_seed, _ptr(self.hits), nol,

@@ -241,6 +241,26 @@ int si_walk_sorted(const void* packed, int work_is_float, int Zc, int Yc,
  * ranges. */
 int si_walk_sorted_set_range(unsigned long long walks_per_range);
 
+/* Selects how the sorted walkers' sweep kernels map walkers to threads:
+ * 0 = one walker per thread; 1 (default) = two consecutive walkers per
+ * thread, advanced together so each thread keeps two record gathers in
+ * flight; 2 = three walkers per thread; 3 = four (si_walk_sorted only; the
+ * batched walker pairs walkers for every mode but 0). Process-wide; speed
+ * only (the hit maps do not depend on it). */
+int si_walk_sorted_set_pairs(int pairs);
+
+/* Selects where si_walk_sorted's sweep loop runs: 1 (default) = on the
+ * device, as a CUDA graph per seed range whose WHILE node repeats
+ * (scatter, sweep, scan) rounds while walkers are live, with no host round
+ * trip per sweep; 0 = on the host, reading the live count back after every
+ * scan. Process-wide; the hit maps do not depend on it. */
+int si_walk_sorted_set_loop(int device_loop);
+
+/* Most sweeps one si_walk_sorted call may run (0 = 2^24, the default); a
+ * walk that would need more stops there and the call returns SI_ERR_LIMIT.
+ * The device loop checks it after every two sweeps. */
+int si_walk_sorted_set_round_limit(unsigned long long sweeps);
+
 /* Walker on the reference's own random stream: the same walk as si_walk
  * (packed records, weights, border rule, one uint32 hit per accepted move)
  * with u drawn from the reference walker's binary32 "MRG32k3a" recurrence

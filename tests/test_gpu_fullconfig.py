@@ -166,6 +166,83 @@ def test_many_seed_ranges_and_sweep_lengths(sweep_steps, cuda):
     assert got.shape == exp["hits"].shape and np.array_equal(got, exp["hits"])
 
 
+@pytest.mark.parametrize("mode", [0, 1, 2, 3])
+@pytest.mark.parametrize("is_float", [False, True], ids=["u8", "f32"])
+def test_sweep_modes_bit_exact(mode, is_float, cuda):
+    """Every sweep-kernel mapping (1, 2, 3 or 4 walkers per thread,
+    si_walk_sorted_set_pairs) gives the oracle's hit maps bit for bit, with
+    walk ends that are not multiples of four steps (sorw = 150, sweeps of 13
+    steps: the paired loop's unaligned head and tail) on uint8 and float
+    volumes."""
+    img, lab, _ = plain_volume(seed=4, shape=(30, 34, 37), z_every=5, semi=(6, 12))
+    if is_float:
+        img = img.astype(np.float32) * 1.7 + 3.0
+    key = 91
+    kw = dict(nbrw=3, sorw=150)
+    exp = O.smart_interpolation(img, lab, return_hits=True, key=key, **kw)
+    nat.call("si_walk_sorted_set_pairs", mode)
+    try:
+        got = smart_interpolation(img, lab, return_hits=True, rng_seed=key, sweep_steps=13, **kw)
+    finally:
+        nat.call("si_walk_sorted_set_pairs", 1)
+    assert np.array_equal(got["hits"], exp["hits"]) and np.array_equal(got["regular"], exp["regular"])
+
+
+@pytest.mark.parametrize("device_loop", [1, 0], ids=["device_loop", "host_loop"])
+def test_sweep_loops_bit_exact(device_loop, cuda):
+    """The device-side sweep loop (a WHILE graph per seed range) and the host
+    loop give the oracle's hit maps, also over several seed ranges, and report
+    the same number of sweeps."""
+    img, lab, _ = plain_volume(seed=7, shape=(32, 36, 30), z_every=5, semi=(6, 11))
+    key = 5
+    kw = dict(nbrw=2, sorw=600)
+    exp = O.smart_interpolation(img, lab, return_hits=True, key=key, **kw)
+    rounds = {}
+    for ranges in (1, 4):
+        d, l = I.normalize_host_dtypes(img, lab)
+        ti, tl = I.upload(d, l)
+        job = I.DeviceJob(ti, I._IMG_DTYPES[d.dtype], tl, I._LAB_DTYPES[l.dtype], rng_seed=key, **kw)
+        assert job.analyze() is None
+        job.prepare()
+        walks = int(job.n_seeds.item()) * kw["nbrw"]
+        nat.call("si_walk_sorted_set_loop", device_loop)
+        nat.call("si_walk_sorted_set_range", walks // ranges + 1 if ranges > 1 else 0)
+        try:
+            job.walk()
+        finally:
+            nat.call("si_walk_sorted_set_loop", 1)
+            nat.call("si_walk_sorted_set_range", 0)
+        assert np.array_equal(job.hits_full().cpu().numpy(), exp["hits"]), ranges
+        rounds[ranges] = job.rounds
+    sweeps = -(-kw["sorw"] // 32)
+    assert rounds[1] == sweeps and rounds[4] >= 3 * sweeps, rounds
+
+
+@pytest.mark.parametrize("device_loop", [1, 0], ids=["device_loop", "host_loop"])
+def test_sweep_round_limit_runs_out(device_loop, cuda):
+    """With the round limit below what the walk needs, the walk stops there
+    and reports SI_ERR_LIMIT; with the default limit the same job on the same
+    context is correct again."""
+    img, lab, _ = plain_volume(seed=8, shape=(24, 28, 26), z_every=5, semi=(5, 9))
+    kw = dict(nbrw=1, sorw=400)
+    d, l = I.normalize_host_dtypes(img, lab)
+    ti, tl = I.upload(d, l)
+    job = I.DeviceJob(ti, I._IMG_DTYPES[d.dtype], tl, I._LAB_DTYPES[l.dtype], rng_seed=3, **kw)
+    assert job.analyze() is None
+    job.prepare()
+    nat.call("si_walk_sorted_set_loop", device_loop)
+    nat.call("si_walk_sorted_set_round_limit", 3)
+    try:
+        with pytest.raises(RuntimeError, match="no convergence"):
+            job.walk()
+    finally:
+        nat.call("si_walk_sorted_set_round_limit", 0)
+        nat.call("si_walk_sorted_set_loop", 1)
+    got = smart_interpolation(img, lab, return_hits=True, rng_seed=3, **kw)
+    exp = O.smart_interpolation(img, lab, return_hits=True, key=3, **kw)
+    assert np.array_equal(got["hits"], exp["hits"])
+
+
 @pytest.mark.parametrize("allaxis", [False, True])
 def test_reference_stream_bit_exact_against_oracle(allaxis, cuda):
     """rng='reference': hit maps and labels equal the oracle's walk with the
