@@ -1096,7 +1096,9 @@ __global__ void __launch_bounds__(256) bbucket_kernel(const uint4* __restrict__ 
                                                       const VolDesc* __restrict__ vols, int n_vols, int sorw,
                                                       int edge, uint32_t* __restrict__ counts,
                                                       const uint32_t* __restrict__ offsets,
-                                                      uint4* __restrict__ states_out) {
+                                                      uint4* __restrict__ states_out,
+                                                      const uint32_t* __restrict__ n_dev = nullptr) {
+  if (n_dev) n = *n_dev;  // the count lives on the device (device-side sweep loop)
   const int lane = threadIdx.x & 31;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
@@ -1129,7 +1131,9 @@ template <bool kPair, int kMinBlocks>
 __global__ void __launch_bounds__(256, kMinBlocks) bsweep_kernel(const VolDesc* __restrict__ vols_g, int n_vols,
                                                                  uint4* __restrict__ states, uint32_t n_live,
                                                                  uint32_t K, uint32_t k0, uint32_t k1, int edge,
-                                                                 uint32_t* __restrict__ next_counts) {
+                                                                 uint32_t* __restrict__ next_counts,
+                                                                 const uint32_t* __restrict__ live_dev) {
+  if (live_dev) n_live = *live_dev;  // the count lives on the device (device-side sweep loop)
   __shared__ int32_t s_delta[256 * 6];  // move offsets of every volume
   __shared__ VolDesc vols[256];         // the volume table (at most 256 volumes)
   for (int i = threadIdx.x; i < n_vols; i += blockDim.x) vols[i] = vols_g[i];
@@ -1282,7 +1286,7 @@ int make_batch_plan(const si_volume_t* vols, int n_vols, int nbrw, int edge, con
   P.off_sums = off;
   off = si::align_up(off + (nblocks + 1) * sizeof(uint32_t), 256);
   P.off_ctrs = off;
-  off = si::align_up(off + 4 * sizeof(uint32_t), 256);
+  off = si::align_up(off + si::kCtrWords * sizeof(uint32_t), 256);
   P.total = off;
   return SI_OK;
 }
@@ -1346,29 +1350,95 @@ extern "C" int si_walk_sorted_batch(const si_volume_t* vols, int n_vols, int nbr
   const int sms = sm_count();
   const int gb = sms * 8;
   const uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
-  int cur = 0, rounds = 0;
-  uint64_t n_prev = P.walks;
   uint32_t* counts2 = reinterpret_cast<uint32_t*>(base + Pmax.off_counts2);
   const size_t count_bytes = (size_t)(nbt + 1) * sizeof(uint32_t);
+  // walker pairs unless mode 0
+  const bool pairs = g_sweep_pairs.load(std::memory_order_relaxed) != 0;
+  const uint64_t bcap = (uint64_t)sms * 8;
+  auto sweep = [&](cudaStream_t s, uint4* s_in, uint32_t live_now, const uint32_t* live_dev, uint32_t* c_next) {
+    const uint64_t threads = live_dev ? bcap * 256 : (pairs ? ((uint64_t)live_now + 1) / 2 : (uint64_t)live_now);
+    const uint64_t want_blocks = (threads + 255) / 256;
+    const uint32_t blocks = (uint32_t)(want_blocks < bcap ? want_blocks : bcap);
+    if (pairs)  // measured: 2 CTAs of 256 per SM (no spills) beat 3
+      bsweep_kernel<true, 2><<<blocks, 256, 0, s>>>(d_vols, n_vols, s_in, live_now, (uint32_t)sweep_steps, k0, k1,
+                                                    sort_edge, c_next, live_dev);
+    else
+      bsweep_kernel<false, 5><<<blocks, 256, 0, s>>>(d_vols, n_vols, s_in, live_now, (uint32_t)sweep_steps, k0, k1,
+                                                     sort_edge, c_next, live_dev);
+  };
+  auto scan = [&](cudaStream_t s, const uint32_t* c) {
+    scan_sums_kernel<<<nblocks, 256, 0, s>>>(c, nbt, sums);
+    scan_top_kernel<<<1, 1024, 0, s>>>(sums, nblocks);
+    scan_apply_kernel<<<nblocks, 256, 0, s>>>(c, nbt, sums, offsets, ctrs);
+  };
+  if (g_device_loop.load(std::memory_order_relaxed)) {
+    // device-side sweep loop, as in si_walk_sorted
+    const uint32_t limit = round_limit();
+    uint32_t* C0 = counts;
+    uint32_t* C1 = counts2;
+    cudaMemsetAsync(ctrs, 0, kCtrWords * sizeof(uint32_t), st);
+    cudaMemsetAsync(C0, 0, count_bytes, st);
+    bbucket_kernel<true, false><<<gb, 256, 0, st>>>(nullptr, P.walks, d_vols, n_vols, sorw, sort_edge, C0, nullptr,
+                                                    nullptr);
+    scan(st, C0);
+    cudaMemsetAsync(C0, 0, count_bytes, st);
+    cudaMemsetAsync(C1, 0, count_bytes, st);
+    bbucket_kernel<true, true><<<gb, 256, 0, st>>>(nullptr, P.walks, d_vols, n_vols, sorw, sort_edge, C0, offsets,
+                                                   states[0]);
+    sweep(st, states[0], 0u, ctrs, C1);
+    round_shift_kernel<<<1, 1, 0, st>>>(ctrs);
+    scan(st, C1);
+    rc = check_launch("si_walk_sorted_batch: round 0");
+    if (rc) return rc;
+    cudaGraphExec_t exec = nullptr;
+    rc = build_while_graph(
+        [&](cudaStream_t cs, cudaGraphConditionalHandle h) {
+          for (int half = 0; half < 2; ++half) {
+            uint32_t* cur_c = half ? C0 : C1;  // scanned sizes -> scatter cursor
+            uint32_t* nxt_c = half ? C1 : C0;  // the sweep's counts of the round after
+            uint4* s_in = states[half];
+            uint4* s_out = states[1 - half];
+            cudaMemsetAsync(cur_c, 0, count_bytes, cs);
+            cudaMemsetAsync(nxt_c, 0, count_bytes, cs);
+            bbucket_kernel<false, true><<<gb, 256, 0, cs>>>(s_in, 0, d_vols, n_vols, sorw, sort_edge, cur_c, offsets,
+                                                            s_out, ctrs + 3);
+            sweep(cs, s_out, 0u, ctrs, nxt_c);
+            round_shift_kernel<<<1, 1, 0, cs>>>(ctrs);
+            scan(cs, nxt_c);
+          }
+          round_cond_kernel<<<1, 1, 0, cs>>>(ctrs, h, limit);
+        },
+        &exec);
+    if (rc) return rc;
+    if (cudaGraphLaunch(exec, st) != cudaSuccess) rc = set_error(SI_ERR_CUDA, "si_walk_sorted_batch: graph launch");
+    uint32_t host_ctrs[kCtrWords] = {};
+    if (cudaMemcpyAsync(host_ctrs, ctrs, sizeof(host_ctrs), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      rc = rc ? rc : set_error(SI_ERR_CUDA, "si_walk_sorted_batch: %s", cudaGetErrorString(cudaGetLastError()));
+    cudaGraphExecDestroy(exec);
+    if (rc) return rc;
+    if (host_ctrs[5]) return set_error(SI_ERR_LIMIT, "si_walk_sorted_batch: no convergence within %u sweeps", limit);
+    if (rounds_out) *rounds_out = (int)host_ctrs[4];
+    return check_launch("si_walk_sorted_batch");
+  }
+  int cur = 0, rounds = 0;
+  uint64_t n_prev = P.walks;
   // round 0's bucket sizes come from a counting pass over the virtual
   // (volume, seed, walk) triples; every later round's from the previous sweep
   if (cudaMemsetAsync(counts, 0, count_bytes, st) != cudaSuccess)
     return set_error(SI_ERR_CUDA, "si_walk_sorted_batch: memset failed");
   bbucket_kernel<true, false><<<gb, 256, 0, st>>>(nullptr, n_prev, d_vols, n_vols, sorw, sort_edge, counts, nullptr,
                                                   nullptr);
-  // walker pairs unless mode 0
-  const bool pairs = g_sweep_pairs.load(std::memory_order_relaxed) != 0;
   for (;; ++rounds) {
     const bool first = rounds == 0;
-    scan_sums_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums);
-    scan_top_kernel<<<1, 1024, 0, st>>>(sums, nblocks);
-    scan_apply_kernel<<<nblocks, 256, 0, st>>>(counts, nbt, sums, offsets, ctrs);
+    scan(st, counts);
     uint32_t live_now = 0;
     if (cudaMemcpyAsync(&live_now, ctrs, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
       return set_error(SI_ERR_CUDA, "si_walk_sorted_batch: round %d: %s", rounds,
                        cudaGetErrorString(cudaGetLastError()));
     if (live_now == 0) break;
+    if ((uint64_t)rounds >= round_limit()) return set_error(SI_ERR_LIMIT, "si_walk_sorted_batch: no convergence");
     // counts becomes the scatter's per-bucket cursor, counts2 the next round's sizes
     if (cudaMemsetAsync(counts, 0, count_bytes, st) != cudaSuccess ||
         cudaMemsetAsync(counts2, 0, count_bytes, st) != cudaSuccess)
@@ -1381,22 +1451,11 @@ extern "C" int si_walk_sorted_batch(const si_volume_t* vols, int n_vols, int nbr
       bbucket_kernel<false, true><<<gb, 256, 0, st>>>(states[cur], n_prev, d_vols, n_vols, sorw, sort_edge, counts,
                                                       offsets, states[nxt]);
     cur = nxt;
-    const uint64_t threads = pairs ? ((uint64_t)live_now + 1) / 2 : (uint64_t)live_now;
-    const uint64_t want_blocks = (threads + 255) / 256;
-    const uint32_t blocks = (uint32_t)(want_blocks < (uint64_t)sms * 8 ? want_blocks : (uint64_t)sms * 8);
-#define SI_BSWEEP(P, B)                                                                                         \
-  bsweep_kernel<P, B><<<blocks, 256, 0, st>>>(d_vols, n_vols, states[cur], live_now, (uint32_t)sweep_steps, k0, k1, \
-                                              sort_edge, counts2)
-    if (pairs)
-      SI_BSWEEP(true, 2);  // measured: 2 CTAs of 256 per SM (no spills) beat 3
-    else
-      SI_BSWEEP(false, 5);
-#undef SI_BSWEEP
+    sweep(st, states[cur], live_now, nullptr, counts2);
     rc = check_launch("si_walk_sorted_batch: sweep");
     if (rc) return rc;
     std::swap(counts, counts2);
     n_prev = live_now;
-    if (rounds > (1 << 24)) return set_error(SI_ERR_LIMIT, "si_walk_sorted_batch: no convergence");
   }
   if (rounds_out) *rounds_out = rounds;
   return check_launch("si_walk_sorted_batch");

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+from biomedisa_gb300 import _native as nat
 from biomedisa_gb300 import smart_interpolation, smart_interpolation_batch
 from biomedisa_gb300.synthetic import batch_volumes, plain_volume
 
@@ -25,13 +26,22 @@ def _volumes():
     return imgs, labs
 
 
-@pytest.mark.parametrize("graph", [True, False])
-def test_batch_equals_single_and_oracle(graph, cuda, tmp_path, monkeypatch):
+@pytest.mark.parametrize("graph,device_loop,pairs", [(True, 1, 1), (False, 1, 1), (True, 0, 1), (True, 1, 0)],
+                         ids=["graph", "no_graph", "host_loop", "one_walker_per_thread"])
+def test_batch_equals_single_and_oracle(graph, device_loop, pairs, cuda, tmp_path, monkeypatch):
+    """Also with the host-side sweep loop and with one walker per thread
+    (the defaults are the device loop and walker pairs)."""
     monkeypatch.setenv("SI_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
     imgs, labs = _volumes()
     kw = dict(nbrw=2, sorw=90, smooth=3, uncertainty=True, return_hits=True)
     rep = {}
-    got = smart_interpolation_batch(imgs, labs, rng_seed=11, graph=graph, report=rep, **kw)
+    nat.call("si_walk_sorted_set_loop", device_loop)
+    nat.call("si_walk_sorted_set_pairs", pairs)
+    try:
+        got = smart_interpolation_batch(imgs, labs, rng_seed=11, graph=graph, report=rep, **kw)
+    finally:
+        nat.call("si_walk_sorted_set_loop", 1)
+        nat.call("si_walk_sorted_set_pairs", 1)
     assert rep["sweeps"] > 0 and rep["sort_edge"] > 0
     assert len(got) == len(imgs)
     for img, lab, g in zip(imgs, labs, got):
