@@ -88,6 +88,7 @@ _SIGNATURES = {
     "si_smooth": [_c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
     "si_smooth_tmp_floats": [_c_int, _c_int, _c_int, _c_void_p],
     "si_smooth_status": [_c_void_p, _c_void_p],
+    "si_smooth_set_pairs": [_c_int],
     "si_set_wait_limit": [ctypes.c_longlong],
     "si_geo_normalize": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_void_p, _c_void_p],
     "si_geo_masks": [_c_void_p, _c_int, _c_u64, _c_void_p, _c_int, _c_void_p, _c_void_p],

@@ -1,6 +1,7 @@
 // Post-walk kernels: per-voxel argmax (+ optional uncertainty), label remap
 // and curvature smoothing.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 
 #include "si_common.cuh"
@@ -167,16 +168,26 @@ __global__ void __launch_bounds__(256) remap_kernel(uint8_t* __restrict__ out, P
 // outside it do nothing (or write zeros, when their destination may hold
 // older values).
 // ---------------------------------------------------------------------------
-constexpr int kSX = 64, kSY = 8, kSZ = 32;
-constexpr int kBoxX = kSX + 8, kBoxY = kSY + 2;
-constexpr int kPlaneFloats = kBoxX * kBoxY;  // 720 floats = 2880 bytes per plane
-constexpr int kSlotFloats = 736;             // 2944 bytes: slots 128-byte aligned
+// kP packed pairs per thread: the CTA's column is 64 * kP voxels wide
+// (voxels x0 + tx + 32 j, j < 2 kP; pair p = columns 2p and 2p + 1).
+constexpr int kSY = 8, kSZ = 32;
+template <int kP>
+struct SmoothTile {
+  static constexpr int kSX = 64 * kP;
+  static constexpr int kBoxX = kSX + 8, kBoxY = kSY + 2;
+  static constexpr int kPlaneFloats = kBoxX * kBoxY;                  // floats per plane box
+  static constexpr int kSlotFloats = (kPlaneFloats + 31) / 32 * 32;  // slots 128-byte aligned
+};
 constexpr int kSlots = 4;
 constexpr int kHeadFloats = 64;              // before the pitched volume in tmp1: the support box
 
 // Sticky status of the smoothing kernels (bit 0: a TMA wait gave up); read
 // and cleared by si_smooth_status.
 __device__ uint32_t g_smooth_status;
+
+// Packed pairs per smoothing thread (si_smooth_set_pairs): 2 = 128-wide
+// columns (default), 1 = 64-wide.
+std::atomic<int> g_smooth_pairs{2};
 
 inline int pitch4(int x) { return (x + 3) & ~3; }
 
@@ -230,24 +241,28 @@ __global__ void __launch_bounds__(256) smooth_convert_kernel(const void* __restr
   }
 }
 
-template <bool kF64>
-__global__ void __launch_bounds__(256, 3) smooth_tma_kernel(const __grid_constant__ CUtensorMap src,
-                                                            float* __restrict__ dst, int dst_pitch, int Zc, int Yc,
-                                                            int Xc, const int* __restrict__ box, int grow,
-                                                            int write_outside, uint32_t wait_lim) {
-  __shared__ __align__(128) float pl[kSlots][kSlotFloats];
+template <bool kF64, int kP>
+__global__ void __launch_bounds__(256, kP == 1 ? 3 : 2) smooth_tma_kernel(const __grid_constant__ CUtensorMap src,
+                                                                         float* __restrict__ dst, int dst_pitch,
+                                                                         int Zc, int Yc, int Xc,
+                                                                         const int* __restrict__ box, int grow,
+                                                                         int write_outside, uint32_t wait_lim) {
+  using T = SmoothTile<kP>;
+  constexpr int kBoxX = T::kBoxX;
+  __shared__ __align__(128) float pl[kSlots][T::kSlotFloats];
   __shared__ __align__(8) uint64_t bar[kSlots];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int x0 = blockIdx.x * kSX, y0 = blockIdx.y * kSY, zb = blockIdx.z * kSZ;
+  const int x0 = blockIdx.x * T::kSX, y0 = blockIdx.y * kSY, zb = blockIdx.z * kSZ;
   const int ze = min(zb + kSZ, Zc);
-  const int y = y0 + ty, xa = x0 + tx, xb = x0 + 32 + tx;
+  const int y = y0 + ty;
   const size_t dF = (size_t)Yc * dst_pitch;
-  if (box_outside(box, grow, zb, ze - 1, y0, min(y0 + kSY, Yc) - 1, x0, min(x0 + kSX, Xc) - 1)) {
+  if (box_outside(box, grow, zb, ze - 1, y0, min(y0 + kSY, Yc) - 1, x0, min(x0 + T::kSX, Xc) - 1)) {
     if (write_outside && y < Yc) {
       for (int z = zb; z < ze; ++z) {
         float* row = dst + (size_t)z * dF + (size_t)y * dst_pitch;
-        if (xa < Xc) row[xa] = 0.0f;
-        if (xb < Xc) row[xb] = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 2 * kP; ++j)
+          if (x0 + tx + 32 * j < Xc) row[x0 + tx + 32 * j] = 0.0f;
       }
     }
     return;
@@ -262,13 +277,14 @@ __global__ void __launch_bounds__(256, 3) smooth_tma_kernel(const __grid_constan
   if (threadIdx.x == 0) {
     fence_proxy_async_shared();
     for (; issued < kSlots && issued < nq; ++issued) {
-      mbar_expect_tx(&bar[issued], kPlaneFloats * (uint32_t)sizeof(float));
+      mbar_expect_tx(&bar[issued], T::kPlaneFloats * (uint32_t)sizeof(float));
       tma_load_box(pl[issued], &src, x0 - 4, y0 - 1, zb - 1 + issued, &bar[issued]);
     }
   }
   const int ly = ty + 1;
-  const int ia = ly * kBoxX + tx + 4, ib = ia + 32;
-  auto cross = [&](const float* P, uint64_t& cc, uint64_t& xm, uint64_t& xp, uint64_t& ym, uint64_t& yp) {
+  const int i0 = ly * kBoxX + tx + 4;  // column j of the thread sits at i0 + 32 j
+  auto cross = [&](const float* P, int p, uint64_t& cc, uint64_t& xm, uint64_t& xp, uint64_t& ym, uint64_t& yp) {
+    const int ia = i0 + 64 * p, ib = ia + 32;
     cc = f2_pack(P[ia], P[ib]);
     xm = f2_pack(P[ia - 1], P[ib - 1]);
     xp = f2_pack(P[ia + 1], P[ib + 1]);
@@ -277,68 +293,78 @@ __global__ void __launch_bounds__(256, 3) smooth_tma_kernel(const __grid_constan
   };
   auto wait_q = [&](int q) { return mbar_wait_bounded(&bar[q & 3], (uint32_t)(q >> 2) & 1u, wait_lim); };
 
-  uint64_t m_c = 0, m_xm = 0, m_xp = 0, m_ym = 0, m_yp = 0;  // plane z-1
-  uint64_t c_c = 0, c_xm = 0, c_xp = 0, c_ym = 0, c_yp = 0;  // plane z
+  uint64_t m_c[kP], m_xm[kP], m_xp[kP], m_ym[kP], m_yp[kP];  // plane z-1
+  uint64_t c_c[kP], c_xm[kP], c_xp[kP], c_ym[kP], c_yp[kP];  // plane z
+#pragma unroll
+  for (int p = 0; p < kP; ++p) m_c[p] = m_xm[p] = m_xp[p] = m_ym[p] = m_yp[p] = c_c[p] = c_xm[p] = c_xp[p] = c_ym[p] =
+      c_yp[p] = 0;
   bool ok = wait_q(0);
   ok = ok && wait_q(1);
   if (ok) {
-    cross(pl[0], m_c, m_xm, m_xp, m_ym, m_yp);
-    cross(pl[1], c_c, c_xm, c_xp, c_ym, c_yp);
+#pragma unroll
+    for (int p = 0; p < kP; ++p) {
+      cross(pl[0], p, m_c[p], m_xm[p], m_xp[p], m_ym[p], m_yp[p]);
+      cross(pl[1], p, c_c[p], c_xm[p], c_xp[p], c_ym[p], c_yp[p]);
+    }
   }
   const uint64_t two = f2_splat(2.0f), half = f2_splat(0.5f), quarter = f2_splat(0.25f);
   const uint64_t eps = f2_splat(1e-10f), hundredth = f2_splat(0.01f);
   const uint64_t nz = f2_negzero();  // products as fma(a, b, -0): never fused into a later sum
   const bool row_in = y < Yc, row_interior = y > 0 && y < Yc - 1;
-  const bool a_in = row_in && xa < Xc, b_in = row_in && xb < Xc;
-  const bool a_int = row_interior && xa > 0 && xa < Xc - 1, b_int = row_interior && xb > 0 && xb < Xc - 1;
   for (int k = 0; k < ze - zb; ++k) {
     const int z = zb + k;
     ok = ok && wait_q(k + 2);
     if (ok) {
       const float* C = pl[(k + 1) & 3];
-      const uint64_t k_mm = f2_pack(C[ia - kBoxX - 1], C[ib - kBoxX - 1]);
-      const uint64_t k_pp = f2_pack(C[ia + kBoxX + 1], C[ib + kBoxX + 1]);
-      const uint64_t k_mp = f2_pack(C[ia - kBoxX + 1], C[ib - kBoxX + 1]);
-      const uint64_t k_pm = f2_pack(C[ia + kBoxX - 1], C[ib + kBoxX - 1]);
-      uint64_t p_c, p_xm, p_xp, p_ym, p_yp;  // plane z+1
-      cross(pl[(k + 2) & 3], p_c, p_xm, p_xp, p_ym, p_yp);
-      const uint64_t c2 = f2_mul(two, c_c, nz);
-      const uint64_t dx = f2_mul(f2_sub(c_xm, c_xp), half, nz);
-      const uint64_t dxx = f2_add(f2_sub(c_xm, c2), c_xp);
-      const uint64_t dx2 = f2_mul(dx, dx, nz);
-      const uint64_t dy = f2_mul(f2_sub(c_ym, c_yp), half, nz);
-      const uint64_t dyy = f2_add(f2_sub(c_ym, c2), c_yp);
-      const uint64_t dy2 = f2_mul(dy, dy, nz);
-      const uint64_t dz = f2_mul(f2_sub(m_c, p_c), half, nz);
-      const uint64_t dzz = f2_add(f2_sub(m_c, c2), p_c);
-      const uint64_t dz2 = f2_mul(dz, dz, nz);
-      const uint64_t dxy = f2_mul(f2_sub(f2_sub(f2_add(k_mm, k_pp), k_mp), k_pm), quarter, nz);
-      const uint64_t dxz = f2_mul(f2_sub(f2_sub(f2_add(p_xm, m_xp), p_xp), m_xm), quarter, nz);
-      const uint64_t dyz = f2_mul(f2_sub(f2_sub(f2_add(p_ym, m_yp), p_yp), m_ym), quarter, nz);
-      uint64_t num = f2_add(f2_mul(dxx, f2_add(dy2, dz2), nz), f2_mul(dyy, f2_add(dx2, dz2), nz));
-      num = f2_add(num, f2_mul(dzz, f2_add(dx2, dy2), nz));
-      num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dx, nz), dy, nz), dxy, nz));
-      num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dx, nz), dz, nz), dxz, nz));
-      num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dy, nz), dz, nz), dyz, nz));
-      const uint64_t den = f2_add(f2_add(f2_add(dx2, dy2), dz2), eps);
-      float na, nb, da, db, ca, cb;
-      f2_unpack(num, na, nb);
-      f2_unpack(den, da, db);
-      f2_unpack(c_c, ca, cb);
-      const float ka = __fdiv_rn(na, da), kb = __fdiv_rn(nb, db);
-      float oa, ob;
-      if (kF64) {
-        oa = __double2float_rn(__dadd_rn((double)ca, __dmul_rn(0.01, (double)ka)));
-        ob = __double2float_rn(__dadd_rn((double)cb, __dmul_rn(0.01, (double)kb)));
-      } else {
-        f2_unpack(f2_add(c_c, f2_mul(hundredth, f2_pack(ka, kb), nz)), oa, ob);
-      }
+      const float* Pn = pl[(k + 2) & 3];
       const bool z_int = z > 0 && z < Zc - 1;
       float* row = dst + (size_t)z * dF + (size_t)y * dst_pitch;
-      if (a_in) row[xa] = (z_int && a_int) ? oa : ca;
-      if (b_in) row[xb] = (z_int && b_int) ? ob : cb;
-      m_c = c_c; m_xm = c_xm; m_xp = c_xp; m_ym = c_ym; m_yp = c_yp;
-      c_c = p_c; c_xm = p_xm; c_xp = p_xp; c_ym = p_ym; c_yp = p_yp;
+#pragma unroll
+      for (int p = 0; p < kP; ++p) {
+        const int ia = i0 + 64 * p, ib = ia + 32;
+        const uint64_t k_mm = f2_pack(C[ia - kBoxX - 1], C[ib - kBoxX - 1]);
+        const uint64_t k_pp = f2_pack(C[ia + kBoxX + 1], C[ib + kBoxX + 1]);
+        const uint64_t k_mp = f2_pack(C[ia - kBoxX + 1], C[ib - kBoxX + 1]);
+        const uint64_t k_pm = f2_pack(C[ia + kBoxX - 1], C[ib + kBoxX - 1]);
+        uint64_t p_c, p_xm, p_xp, p_ym, p_yp;  // plane z+1
+        cross(Pn, p, p_c, p_xm, p_xp, p_ym, p_yp);
+        const uint64_t c2 = f2_mul(two, c_c[p], nz);
+        const uint64_t dx = f2_mul(f2_sub(c_xm[p], c_xp[p]), half, nz);
+        const uint64_t dxx = f2_add(f2_sub(c_xm[p], c2), c_xp[p]);
+        const uint64_t dx2 = f2_mul(dx, dx, nz);
+        const uint64_t dy = f2_mul(f2_sub(c_ym[p], c_yp[p]), half, nz);
+        const uint64_t dyy = f2_add(f2_sub(c_ym[p], c2), c_yp[p]);
+        const uint64_t dy2 = f2_mul(dy, dy, nz);
+        const uint64_t dz = f2_mul(f2_sub(m_c[p], p_c), half, nz);
+        const uint64_t dzz = f2_add(f2_sub(m_c[p], c2), p_c);
+        const uint64_t dz2 = f2_mul(dz, dz, nz);
+        const uint64_t dxy = f2_mul(f2_sub(f2_sub(f2_add(k_mm, k_pp), k_mp), k_pm), quarter, nz);
+        const uint64_t dxz = f2_mul(f2_sub(f2_sub(f2_add(p_xm, m_xp[p]), p_xp), m_xm[p]), quarter, nz);
+        const uint64_t dyz = f2_mul(f2_sub(f2_sub(f2_add(p_ym, m_yp[p]), p_yp), m_ym[p]), quarter, nz);
+        uint64_t num = f2_add(f2_mul(dxx, f2_add(dy2, dz2), nz), f2_mul(dyy, f2_add(dx2, dz2), nz));
+        num = f2_add(num, f2_mul(dzz, f2_add(dx2, dy2), nz));
+        num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dx, nz), dy, nz), dxy, nz));
+        num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dx, nz), dz, nz), dxz, nz));
+        num = f2_sub(num, f2_mul(f2_mul(f2_mul(two, dy, nz), dz, nz), dyz, nz));
+        const uint64_t den = f2_add(f2_add(f2_add(dx2, dy2), dz2), eps);
+        float na, nb, da, db, ca, cb;
+        f2_unpack(num, na, nb);
+        f2_unpack(den, da, db);
+        f2_unpack(c_c[p], ca, cb);
+        const float ka = __fdiv_rn(na, da), kb = __fdiv_rn(nb, db);
+        float oa, ob;
+        if (kF64) {
+          oa = __double2float_rn(__dadd_rn((double)ca, __dmul_rn(0.01, (double)ka)));
+          ob = __double2float_rn(__dadd_rn((double)cb, __dmul_rn(0.01, (double)kb)));
+        } else {
+          f2_unpack(f2_add(c_c[p], f2_mul(hundredth, f2_pack(ka, kb), nz)), oa, ob);
+        }
+        const int xa = x0 + tx + 64 * p, xb = xa + 32;
+        if (row_in && xa < Xc) row[xa] = (z_int && row_interior && xa > 0 && xa < Xc - 1) ? oa : ca;
+        if (row_in && xb < Xc) row[xb] = (z_int && row_interior && xb > 0 && xb < Xc - 1) ? ob : cb;
+        m_c[p] = c_c[p]; m_xm[p] = c_xm[p]; m_xp[p] = c_xp[p]; m_ym[p] = c_ym[p]; m_yp[p] = c_yp[p];
+        c_c[p] = p_c; c_xm[p] = p_xm; c_xp[p] = p_xp; c_ym[p] = p_ym; c_yp[p] = p_yp;
+      }
     }
     if (__syncthreads_or(!ok)) {
       // a wait gave up: let the copies still in flight land (bounded) before
@@ -353,7 +379,7 @@ __global__ void __launch_bounds__(256, 3) smooth_tma_kernel(const __grid_constan
     // the slot of plane q = k was last read in step k - 1 (or the prologue): refill it
     if (threadIdx.x == 0 && issued < nq) {
       fence_proxy_async_shared();
-      mbar_expect_tx(&bar[issued & 3], kPlaneFloats * (uint32_t)sizeof(float));
+      mbar_expect_tx(&bar[issued & 3], T::kPlaneFloats * (uint32_t)sizeof(float));
       tma_load_box(pl[issued & 3], &src, x0 - 4, y0 - 1, zb - 1 + issued, &bar[issued & 3]);
       ++issued;
     }
@@ -414,14 +440,14 @@ namespace {
 
 // Tensor map over a pitched float32 volume (Zc, Yc, Xp) with logical extents
 // (Zc, Yc, Xc): reads beyond Xc, Yc, Zc or below 0 return zero.
-int encode_volume_map(CUtensorMap* map, float* base, int Zc, int Yc, int Xc, const char* what) {
+int encode_volume_map(CUtensorMap* map, float* base, int Zc, int Yc, int Xc, int box_x, const char* what) {
   const EncodeTiledFn enc = encode_fn();
   if (!enc) return set_error(SI_ERR_CUDA, "%s: cuTensorMapEncodeTiled unavailable", what);
   std::memset(map, 0, sizeof(*map));
   const int Xp = pitch4(Xc);
   const cuuint64_t dims[3] = {(cuuint64_t)Xc, (cuuint64_t)Yc, (cuuint64_t)Zc};
   const cuuint64_t strides[2] = {(cuuint64_t)Xp * sizeof(float), (cuuint64_t)Xp * Yc * sizeof(float)};
-  const cuuint32_t boxd[3] = {kBoxX, kBoxY, 1};
+  const cuuint32_t boxd[3] = {(cuuint32_t)box_x, (cuuint32_t)(kSY + 2), 1};
   const cuuint32_t estr[3] = {1, 1, 1};
   const CUresult cr = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, boxd, estr,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -443,14 +469,17 @@ int smooth_maps(void* maps, float* tmp0, float* tmp1, int nol, int Zc, int Yc, i
   float* tmp1v = tmp1 + kHeadFloats;
   if (iters > 0 && ((reinterpret_cast<uintptr_t>(tmp0) | reinterpret_cast<uintptr_t>(tmp1)) & 15u))
     return set_error(SI_ERR_ARG, "%s: tmp0/tmp1 must be 16-byte aligned", what);
+  // pairs per thread: 2 (128-wide columns) unless the rows are short
+  const int kp = g_smooth_pairs.load(std::memory_order_relaxed) == 1 || Xc <= 64 ? 1 : 2;
+  const int sx = 64 * kp;
   CUtensorMap map0, map1;
   if (iters > 0) {
-    int rc = encode_volume_map(&map0, tmp0, Zc, Yc, Xc, what);
+    int rc = encode_volume_map(&map0, tmp0, Zc, Yc, Xc, sx + 8, what);
     if (rc) return rc;
-    rc = encode_volume_map(&map1, tmp1v, Zc, Yc, Xc, what);
+    rc = encode_volume_map(&map1, tmp1v, Zc, Yc, Xc, sx + 8, what);
     if (rc) return rc;
   }
-  const dim3 grid((Xc + kSX - 1) / kSX, (Yc + kSY - 1) / kSY, (Zc + kSZ - 1) / kSZ);
+  const dim3 grid((Xc + sx - 1) / sx, (Yc + kSY - 1) / kSY, (Zc + kSZ - 1) / kSZ);
   const int cgrid = std::max(1, std::min(sm_count() * 8, (Zc * Yc + 7) / 8));
   const uint32_t wl = wait_limit();
   for (int l = 0; l < nol; ++l) {
@@ -471,10 +500,20 @@ int smooth_maps(void* maps, float* tmp0, float* tmp1, int nol, int Zc, int Yc, i
       // only iteration 1's destination (tmp1) may hold another map's values
       // outside the support; every later destination is +0 there already
       const int write_outside = (it == 1 && !last) ? 1 : 0;
-      if (update)
-        smooth_tma_kernel<true><<<grid, 256, 0, st>>>(sm, dst, pitch, Zc, Yc, Xc, box, it, write_outside, wl);
-      else
-        smooth_tma_kernel<false><<<grid, 256, 0, st>>>(sm, dst, pitch, Zc, Yc, Xc, box, it, write_outside, wl);
+#define SI_SMOOTH(F64, P) \
+  smooth_tma_kernel<F64, P><<<grid, 256, 0, st>>>(sm, dst, pitch, Zc, Yc, Xc, box, it, write_outside, wl)
+      if (update) {
+        if (kp == 2)
+          SI_SMOOTH(true, 2);
+        else
+          SI_SMOOTH(true, 1);
+      } else {
+        if (kp == 2)
+          SI_SMOOTH(false, 2);
+        else
+          SI_SMOOTH(false, 1);
+      }
+#undef SI_SMOOTH
     }
   }
   return check_launch(what);
@@ -516,6 +555,13 @@ extern "C" int si_smooth_f32(float* maps, float* tmp0, float* tmp1, int nol, int
   const int rc = smooth_args(maps, tmp0, tmp1, nol, Zc, Yc, Xc, iters, update, "si_smooth_f32");
   if (rc) return rc;
   return smooth_maps<false>(maps, tmp0, tmp1, nol, Zc, Yc, Xc, iters, update, as_stream(stream), "si_smooth_f32");
+}
+
+extern "C" int si_smooth_set_pairs(int pairs) {
+  clear_error();
+  if (pairs < 1 || pairs > 2) return set_error(SI_ERR_ARG, "si_smooth_set_pairs: 1 or 2");
+  g_smooth_pairs.store(pairs, std::memory_order_relaxed);
+  return SI_OK;
 }
 
 extern "C" int si_smooth_status(int* status, void* stream) {

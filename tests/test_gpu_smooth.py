@@ -95,6 +95,21 @@ def test_pipeline_reference_update_bit_exact(cuda):
     assert np.mean(f32["smooth"] == got["smooth"]) > 0.99
 
 
+@pytest.mark.parametrize("pairs", [1, 2])
+@pytest.mark.parametrize("shape", [(9, 13, 70), (20, 17, 200), (6, 11, 129)], ids=["x70", "x200", "x129"])
+def test_tile_widths_bit_exact(pairs, shape, cuda):
+    """Both column widths of the smoothing kernel (64 and 128 voxels per CTA)
+    give the oracle's maps, on rows that end inside a column."""
+    maps = _maps(shape, 2, False, seed=sum(shape) + pairs)
+    nat.call("si_smooth_set_pairs", pairs)
+    try:
+        for update in ("f32", "ref_f64"):
+            got = _run(maps, 3, update, hits=False)
+            assert np.array_equal(got.view(np.uint32), O.smooth(maps, 3, update).view(np.uint32)), update
+    finally:
+        nat.call("si_smooth_set_pairs", 2)
+
+
 def test_wait_limit_runs_out_and_reports(cuda):
     """With the wait limit at 0 spins every TMA wait of the smoothing kernels
     gives up at once; the kernels let their copies land, record the status
