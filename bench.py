@@ -320,6 +320,9 @@ def main():
     ap.add_argument("--nbrw", type=int, default=None, help="override (profiling only)")
     ap.add_argument("--sorw", type=int, default=None, help="override (profiling only)")
     ap.add_argument("--smooth", type=int, default=None, help="override (profiling only)")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="profiling only: run the walker's sweep loop from the host (same kernels, one launch per "
+                         "sweep) so that a profiler sees the kernels the device-side loop runs inside a graph")
     args = ap.parse_args()
     wl = dict(WORKLOADS[args.workload])
     for k in ("nbrw", "sorw", "smooth"):
@@ -327,6 +330,8 @@ def main():
             if not args.profile_jobs:
                 ap.error(f"--{k} is only allowed with --profile-jobs")
             wl[k] = getattr(args, k)
+    if args.host_loop and not args.profile_jobs:
+        ap.error("--host-loop is only allowed with --profile-jobs")
     if args.profile_jobs:
         profile_jobs(args, wl)
         return
@@ -439,7 +444,9 @@ def main():
         "roofline": {"bound": "l2", "achieved": achieved_l2, "peak": l2_gbs, "unit": "GB/s",
                      "frac": achieved_l2 / l2_gbs if l2_gbs else None, "traffic": traffic,
                      "atomics_per_s": walk_rate, "atomic_peak_per_s": l2["atomics_per_s"],
-                     "note": f"walker (sweep_kernel, {sweeps} launches per job), issue- and L2-bound: "
+                     "atomic_frac": walk_rate / l2["atomics_per_s"] if l2.get("atomics_per_s") else None,
+                     "note": f"walker (sorted-sweep kernel, two walkers per thread, {sweeps} sweeps per job on "
+                             "the device-side loop), issue- and L2-bound: "
                              f"{WALK_SECTORS_L2} x 32 B sectors per step at L2 (one packed neighbourhood record "
                              "+ one hit atomic) x steps / CUDA-event walk duration; peak = L2 read ceiling "
                              "measured in this run by si_probe_l2_read over a 48 MiB L2-resident buffer (no L2 "
@@ -982,6 +989,10 @@ def profile_jobs(args, wl):
     from biomedisa_gb300 import interpolation as I
 
     torch.cuda.set_device(0)
+    if args.host_loop:
+        from biomedisa_gb300 import _native as nat
+
+        nat.call("si_walk_sorted_set_loop", 0)
     img, lab = make_inputs(args.workload)
     data, labels = I.normalize_host_dtypes(img, lab)
     img_t, lab_t = I.upload(data, labels)
