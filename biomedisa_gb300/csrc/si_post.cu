@@ -185,9 +185,10 @@ constexpr int kHeadFloats = 64;              // before the pitched volume in tmp
 // and cleared by si_smooth_status.
 __device__ uint32_t g_smooth_status;
 
-// Packed pairs per smoothing thread (si_smooth_set_pairs): 2 = 128-wide
-// columns (default), 1 = 64-wide.
-std::atomic<int> g_smooth_pairs{2};
+// Packed pairs per smoothing thread (si_smooth_set_pairs): 1 = 64-wide
+// columns (default; measured faster on hit maps, whose support box skips
+// more of the finer columns), 2 = 128-wide (faster on dense maps).
+std::atomic<int> g_smooth_pairs{1};
 
 inline int pitch4(int x) { return (x + 3) & ~3; }
 
@@ -469,7 +470,7 @@ int smooth_maps(void* maps, float* tmp0, float* tmp1, int nol, int Zc, int Yc, i
   float* tmp1v = tmp1 + kHeadFloats;
   if (iters > 0 && ((reinterpret_cast<uintptr_t>(tmp0) | reinterpret_cast<uintptr_t>(tmp1)) & 15u))
     return set_error(SI_ERR_ARG, "%s: tmp0/tmp1 must be 16-byte aligned", what);
-  // pairs per thread: 2 (128-wide columns) unless the rows are short
+  // pairs per thread: 128-wide columns only when selected and the rows are long enough
   const int kp = g_smooth_pairs.load(std::memory_order_relaxed) == 1 || Xc <= 64 ? 1 : 2;
   const int sx = 64 * kp;
   CUtensorMap map0, map1;

@@ -352,9 +352,10 @@ int si_smooth_f32(float* maps, float* tmp0, float* tmp1, int nol, int Zc,
  * the reference. */
 int si_smooth_status(int* status, void* stream);
 
-/* Voxels per thread of the smoothing kernel: pairs = 2 (default) gives each
- * thread four voxels of a 128-wide column, 1 two voxels of a 64-wide one.
- * Process-wide; speed only (results do not depend on it). */
+/* Voxels per thread of the smoothing kernel: pairs = 1 (default) gives each
+ * thread two voxels of a 64-wide column, 2 four voxels of a 128-wide one
+ * (faster on dense maps, slower on sparse hit maps). Process-wide; speed
+ * only (results do not depend on it). */
 int si_smooth_set_pairs(int pairs);
 
 /* Spin limit of every bounded wait on an mbarrier in this library (TMA copies

@@ -107,7 +107,7 @@ def test_tile_widths_bit_exact(pairs, shape, cuda):
             got = _run(maps, 3, update, hits=False)
             assert np.array_equal(got.view(np.uint32), O.smooth(maps, 3, update).view(np.uint32)), update
     finally:
-        nat.call("si_smooth_set_pairs", 2)
+        nat.call("si_smooth_set_pairs", 1)
 
 
 def test_wait_limit_runs_out_and_reports(cuda):
