@@ -187,6 +187,120 @@ __global__ void __launch_bounds__(kTX* kTY) acwe_stencil_kernel(const uint8_t* _
 }
 
 // ---------------------------------------------------------------------------
+// curvop on bit masks. A label's mask is packed once per curvop, 32 voxels
+// of a row per word: M[(z * Y + y) * W + w] bit j = (L[z][y][32 w + j] ==
+// label), W = ceil(X / 32). Each erosion/dilation pass is one thread per
+// word: the 27 neighbour masks are the 9 neighbouring rows' words shifted by
+// one bit (carries from the adjacent words), the nine planes are ANDs of
+// their members, and the pass writes the next mask word. Voxels change in
+// place in L: dilation writes `label` (it reads masks only); erosion writes
+// the last differing neighbour's value, read from L — a non-label voxel,
+// which an erosion pass never changes, so the in-place update is race-free.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) acwe_pack_kernel(const uint8_t* __restrict__ L, int Z, int Y, int X, int W,
+                                                        int label, uint32_t* __restrict__ M) {
+  const int lane = threadIdx.x & 31;
+  const int64_t rows = (int64_t)Z * Y;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < rows; r += nwarps) {
+    const uint8_t* row = L + r * X;
+    uint32_t* mrow = M + r * W;
+    for (int w0 = 0; w0 < W; w0 += 32) {
+      uint32_t mine = 0;  // lane i keeps word w0 + i
+      const int nw = min(32, W - w0);
+      for (int i = 0; i < nw; ++i) {
+        const int x = 32 * (w0 + i) + lane;
+        const bool hit = x < X && row[x] == label;
+        const uint32_t word = __ballot_sync(0xffffffffu, hit);
+        if (lane == i) mine = word;
+      }
+      if (lane < nw) mrow[w0 + lane] = mine;
+    }
+  }
+}
+
+template <bool kErode>
+__global__ void __launch_bounds__(256) acwe_morph_bits_kernel(uint8_t* __restrict__ L,
+                                                              const uint32_t* __restrict__ Min,
+                                                              uint32_t* __restrict__ Mout, int Z, int Y, int X, int W,
+                                                              int label) {
+  const int64_t n = (int64_t)Z * Y * W;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int w = (int)(i % W);
+    const int64_t zy = i / W;
+    const int y = (int)(zy % Y), z = (int)(zy / Y);
+    const uint32_t m = Min[i];
+    if (z < 1 || z > Z - 2 || y < 1 || y > Y - 2) {
+      Mout[i] = m;
+      continue;
+    }
+    // interior columns 1..X-2 of this word
+    const int xa = 32 * w;
+    uint32_t inner = 0xffffffffu;
+    if (xa == 0) inner &= ~1u;
+    const int last = X - 2 - xa;  // highest interior bit
+    if (last < 31) inner &= last >= 0 ? (0xffffffffu >> (31 - last)) : 0u;
+    // neighbour masks S[k], k = (dz+1)*9 + (dy+1)*3 + (dx+1): bit j = voxel
+    // (z+dz, y+dy, xa+j+dx) is the label
+    uint32_t S[27];
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int64_t r = ((int64_t)(z + dz) * Y + (y + dy)) * W;
+        const uint32_t c = Min[r + w];
+        const uint32_t p = w > 0 ? Min[r + w - 1] : 0u;
+        const uint32_t q = w + 1 < W ? Min[r + w + 1] : 0u;
+        const int k = (dz + 1) * 9 + (dy + 1) * 3;
+        S[k] = (c << 1) | (p >> 31);
+        S[k + 1] = c;
+        S[k + 2] = (c >> 1) | (q << 31);
+      }
+    uint32_t cond;
+    if (kErode) {
+      uint32_t all = 0xffffffffu, keep = 0u;
+#pragma unroll
+      for (int k = 0; k < 27; ++k) all &= S[k];
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        uint32_t full = 0xffffffffu;
+#pragma unroll
+        for (int k = 0; k < 27; ++k)
+          if (plane_mask(t) >> k & 1u) full &= S[k];
+        keep |= full;
+      }
+      cond = m & ~all & ~keep & inner;
+      uint32_t todo = cond;
+      while (todo) {
+        const int j = __ffs(todo) - 1;
+        todo &= todo - 1u;
+        // the last neighbour in scan order that is not the label
+        int k = 26;
+        while (k > 0 && (S[k] >> j & 1u)) --k;
+        const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
+        const uint8_t sub = L[((int64_t)(z + dz) * Y + (y + dy)) * X + (xa + j + dx)];
+        L[((int64_t)z * Y + y) * X + xa + j] = sub;
+      }
+      Mout[i] = m & ~cond;
+    } else {
+      uint32_t any = 0u;
+#pragma unroll
+      for (int k = 0; k < 27; ++k) any |= S[k];
+      cond = ~m & any & inner;
+      uint32_t todo = cond;
+      while (todo) {
+        const int j = __ffs(todo) - 1;
+        todo &= todo - 1u;
+        L[((int64_t)z * Y + y) * X + xa + j] = (uint8_t)label;
+      }
+      Mout[i] = m | cond;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Image conversion (img_to_uint8, biomedisa_helper.py:345-352) and gather.
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -603,6 +717,30 @@ extern "C" int si_acwe_curvop(uint8_t* L, uint8_t* tmp, int Z, int Y, int X, int
     return set_error(SI_ERR_ARG, "si_acwe_curvop: bad arguments");
   if (L == tmp) return set_error(SI_ERR_ARG, "si_acwe_curvop: tmp must not alias L");
   cudaStream_t st = as_stream(stream);
+  if (steps == 0) return SI_OK;
+  // bit masks when two of them fit in tmp (rows of at least ~8 voxels):
+  // one pack, then every pass in place on L
+  const int W = (X + 31) / 32;
+  const size_t words = (size_t)Z * Y * W;
+  const size_t mbytes = (words * sizeof(uint32_t) + 255) / 256 * 256;
+  if (2 * mbytes <= (size_t)Z * Y * X && (reinterpret_cast<uintptr_t>(tmp) & 255u) == 0) {
+    uint32_t* M[2] = {reinterpret_cast<uint32_t*>(tmp), reinterpret_cast<uint32_t*>(tmp + mbytes)};
+    const int rows_grid = grid_n((uint64_t)Z * Y * 32, 256);
+    acwe_pack_kernel<<<rows_grid, 256, 0, st>>>(L, Z, Y, X, W, label, M[0]);
+    const int g = grid_n(words, 256);
+    int p = 0;
+    for (int k = 0; k < steps; ++k) {
+      for (int h = 0; h < 2; ++h) {
+        const bool erode = (k % 2 == 0) == (h == 0);
+        if (erode)
+          acwe_morph_bits_kernel<true><<<g, 256, 0, st>>>(L, M[p], M[p ^ 1], Z, Y, X, W, label);
+        else
+          acwe_morph_bits_kernel<false><<<g, 256, 0, st>>>(L, M[p], M[p ^ 1], Z, Y, X, W, label);
+        p ^= 1;
+      }
+    }
+    return check_launch("si_acwe_curvop");
+  }
   uint8_t* buf[2] = {L, tmp};
   int p = 0;
   for (int k = 0; k < steps; ++k) {
