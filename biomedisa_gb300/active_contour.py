@@ -138,8 +138,10 @@ class AcweRun:
         self.launches += 1
         return out
 
-    def refined(self) -> torch.Tensor:
-        """refinement (active_contour.py:204-225), then the crop put back."""
+    def refined(self, scan_events=None) -> torch.Tensor:
+        """refinement (active_contour.py:204-225), then the crop put back.
+        scan_events: optional pair of CUDA events recorded around the chamfer
+        scan (for measurement)."""
         z0, y0, x0, cZ, cY, cX = self.box
         n = cZ * cY * cX
         dist = torch.empty(n, dtype=torch.float32, device=self.dev)
@@ -149,7 +151,11 @@ class AcweRun:
         # geodesic raster scan with cost c + (1 - lamb) |offset| at lamb = 0
         launches = ctypes.c_longlong(0)
         nat.call("si_geo_scan_launches", cZ, cY, cX, 0.0, 1, 0, ctypes.byref(launches))
+        if scan_events:
+            scan_events[0].record()
         nat.call("si_geo_scan", _ptr(dist), _ptr(zero), cZ, cY, cX, 1, 0.0, 1, 0, _stream())
+        if scan_events:
+            scan_events[1].record()
         del zero
         cands = self.all_labels[1:]
         class_lut = np.zeros(256, np.int16)
