@@ -897,7 +897,7 @@ def time_acwe_oracle(img, lab, wl, reps):
 def run_acwe_bench(args, wl):
     """Active contour: value = volume voxels / (both activeContour modes) on
     device-resident inputs; e2e through activeContour with numpy in/out;
-    roofline of the dominant kernel, the refinement's chamfer scan."""
+    roofline of the refinement's chamfer band."""
     import torch
 
     from biomedisa_gb300 import _native as nat
@@ -963,10 +963,9 @@ def run_acwe_bench(args, wl):
         t_e2e.append(time.perf_counter() - t0)
         out_bytes = o1.nbytes + o2.nbytes
     e2e_s = sum(t_e2e) / len(t_e2e)
-    # the chamfer scan: two passes over the crop's interior, each voxel update
-    # reading and writing its distance and reading the (zero) image
-    updates = 2 * max(cZ - 1, 0) * max(cY - 2, 0) * max(cX - 2, 0)
-    bytes_alg = updates * 12
+    # the chamfer band: 10 Jacobi passes, each reading and writing the float32
+    # distance of every crop voxel
+    bytes_alg = 10 * 8 * cZ * cY * cX
     achieved = bytes_alg / (scan_ms / 1e3) / 1e9
     hbm = float(peaks().get("hbm_gbs", 6800.0))
     line = {
@@ -980,10 +979,9 @@ def run_acwe_bench(args, wl):
         "gpu_launches": launches // max(args.steps, 1),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": None, "kernel_ms": scan_ms,
-                     "note": "the refinement's chamfer scan (si_geo_scan, lamb 0, one forward and one backward "
-                             "pass, tiled wavefronts), the dominant part of both modes: 12 B per voxel update "
-                             "(distance read + write, zero image read) x 2 passes over the crop interior / its "
-                             "CUDA-event time; latency-bound by dependent tile wavefronts"},
+                     "note": "the refinement's chamfer band (si_acwe_chamfer_band: 10 Jacobi passes of a "
+                             "27-point min-plus stencil over the crop, each reading and writing 4 B per voxel) / "
+                             "its CUDA-event time"},
         "clocks": clocks.summary(),
     }
     if not args.no_cpu_baseline:

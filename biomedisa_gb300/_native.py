@@ -114,6 +114,7 @@ _SIGNATURES = {
     "si_acwe_curvop": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p],
     "si_acwe_scatter": [_c_void_p, *[_c_int] * 9, _c_void_p, _c_void_p],
     "si_acwe_dist_init": [_c_void_p, _c_u64, _c_void_p, _c_void_p],
+    "si_acwe_chamfer_band": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_void_p],
     "si_acwe_refine_hist": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_void_p,
                             _c_void_p],
     "si_acwe_refine_decide": [_c_void_p, _c_void_p, _c_int, _c_int, _c_void_p, _c_void_p],

@@ -10,13 +10,11 @@ rw_large.py:262-271):
     labels, per-slice Gaussian likelihoods of the band's label and non-label
     intensities, and the per-slice relabelling of the band (:204-225).
 
-All work is device kernels of libsmartinterp (si_acwe_*, si_geo_scan); the
+All work is device kernels of libsmartinterp (si_acwe_*); the
 host computes the crop box and the label list from two small device reads.
 There is no CPU fallback.
 """
 from __future__ import annotations
-
-import ctypes
 
 import numpy as np
 import torch
@@ -141,22 +139,20 @@ class AcweRun:
     def refined(self, scan_events=None) -> torch.Tensor:
         """refinement (active_contour.py:204-225), then the crop put back.
         scan_events: optional pair of CUDA events recorded around the chamfer
-        scan (for measurement)."""
+        band (for measurement)."""
         z0, y0, x0, cZ, cY, cX = self.box
         n = cZ * cY * cX
         dist = torch.empty(n, dtype=torch.float32, device=self.dev)
         nat.call("si_acwe_dist_init", _ptr(self.L), n, _ptr(dist), _stream())
-        zero = torch.zeros(n, dtype=torch.float32, device=self.dev)
-        # the chamfer scan (active_contour.py:45-81, iterations = 1) is the
-        # geodesic raster scan with cost c + (1 - lamb) |offset| at lamb = 0
-        launches = ctypes.c_longlong(0)
-        nat.call("si_geo_scan_launches", cZ, cY, cX, 0.0, 1, 0, ctypes.byref(launches))
+        # the chamfer band (active_contour.py:45-81 and :209-210) by Jacobi
+        # relaxation, exact for every voxel that reaches the result
+        spare = torch.empty(n, dtype=torch.float32, device=self.dev)
         if scan_events:
             scan_events[0].record()
-        nat.call("si_geo_scan", _ptr(dist), _ptr(zero), cZ, cY, cX, 1, 0.0, 1, 0, _stream())
+        nat.call("si_acwe_chamfer_band", _ptr(dist), _ptr(spare), cZ, cY, cX, _stream())
         if scan_events:
             scan_events[1].record()
-        del zero
+        del spare
         cands = self.all_labels[1:]
         class_lut = np.zeros(256, np.int16)
         for j, v in enumerate(cands):
@@ -171,7 +167,7 @@ class AcweRun:
         out = torch.empty((self.Z, self.Y, self.X), dtype=torch.uint8, device=self.dev)
         nat.call("si_acwe_refine_apply", _ptr(dist), _ptr(self.D), _ptr(lut), z0, y0, x0, cZ, cY, cX, self.Z, self.Y,
                  self.X, _ptr(out), _stream())
-        self.launches += 5 + int(launches.value)
+        self.launches += 15
         return out
 
 

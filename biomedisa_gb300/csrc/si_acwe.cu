@@ -2,10 +2,10 @@
 // (biomedisa/features/active_contour.py:109-225 and curvop_numba.py:5-149):
 //   * 'acwe': `steps` rounds of (label means -> evolution -> for every label
 //     `smooth` erosion/dilation pairs);
-//   * 'refined': a chamfer band around the labels (the geodesic raster scan of
-//     si_geo.cu with a zero image and lamb = 0), per-slice Gaussian
-//     likelihoods from band histograms, and a per-slice lookup table that
-//     labels each band voxel by its intensity.
+//   * 'refined': a chamfer band around the labels (distance <= 10, by Jacobi
+//     relaxation: see the refinement section), per-slice Gaussian likelihoods
+//     from band histograms, and a per-slice lookup table that labels each band
+//     voxel by its intensity.
 // Both run on the reference's cropped volume: the image and labels padded by
 // one zero voxel and cut to the labels' bounding box grown by 100 voxels
 // (reduce_blocksize, active_contour.py:84-104), gathered in one pass.
@@ -462,7 +462,77 @@ __global__ void __launch_bounds__(256) acwe_scatter_kernel(const uint8_t* __rest
 
 // ---------------------------------------------------------------------------
 // Refinement (active_contour.py:204-225).
+//
+// The band. The reference runs one forward and one backward chamfer raster
+// scan (weights 1, sqrt2, sqrt3) from 0 on labels / 100 elsewhere and keeps
+// distance <= 10. For every voxel whose band membership reaches the output,
+// that scan gives the exact chamfer distance to the nearest label: an optimal
+// path is monotone in each coordinate, so its moves sort into forward moves
+// (the forward pass's neighbours) followed by backward moves, all inside the
+// box of its ends and so inside both passes' domains. (The crop's boundary
+// rows and columns, never updated by the reference, are never band here
+// either; its first and last planes are padding, whose slices the result
+// drops, or lie at least 100 voxels from any label.) The decision <= 10 does
+// not depend on rounding: path lengths p + q sqrt2 + r sqrt3 within 10 moves
+// are exactly 10 or differ from it by at least 0.0246, far beyond binary32
+// rounding. So the band is computed by Jacobi relaxation instead of the
+// sequential scan: pass k takes each interior voxel's minimum over itself and
+// its 26 neighbours plus the move weights; after 10 passes every path of
+// cost <= 10 (at most 10 moves) has been followed. Values are clamped to 11.
 // ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTX* kTY) acwe_chamfer_pass_kernel(const float* __restrict__ src, int Z, int Y,
+                                                                     int X, float* __restrict__ dst) {
+  constexpr int kRowF = kTX + 2, kPlaneF = (kTY + 2) * kRowF;
+  __shared__ float s[3][kPlaneF];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
+  const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY, zs = blockIdx.z * kZChunk;
+  const int ze = min(zs + kZChunk, Z);
+  auto load_plane = [&](int z, int slot) {
+    for (int i = tid; i < kPlaneF; i += kTX * kTY) {
+      const int r = i / kRowF, c = i - r * kRowF;
+      const int gy = y0 - 1 + r, gx = x0 - 1 + c;
+      float v = 11.0f;
+      if ((unsigned)z < (unsigned)Z && (unsigned)gy < (unsigned)Y && (unsigned)gx < (unsigned)X)
+        v = src[((size_t)z * Y + gy) * X + gx];
+      s[slot][i] = v;
+    }
+  };
+  load_plane(zs - 1, 0);
+  load_plane(zs, 1);
+  const int x = x0 + tx, y = y0 + ty;
+  const bool in_xy = x < X && y < Y;
+  const bool int_xy = x >= 1 && x <= X - 2 && y >= 1 && y <= Y - 2;
+  const int cpos = (ty + 1) * kRowF + tx + 1;
+  const float w1 = 1.0f, w2 = 1.41421356f, w3 = 1.73205081f;
+  int sm = 0, sc = 1, sp = 2;
+  for (int z = zs; z < ze; ++z) {
+    load_plane(z + 1, sp);
+    __syncthreads();
+    if (in_xy) {
+      float best = s[sc][cpos];
+      if (int_xy) {  // every plane of the crop relaxes (see above); rows/columns 0 and n-1 keep their values
+        const float* pl[3] = {s[sm], s[sc], s[sp]};
+#pragma unroll
+        for (int i = 0; i < 27; ++i) {
+          const int dz = i / 9 - 1, dy = (i / 3) % 3 - 1, dx = i % 3 - 1;
+          const int nzero = (dz != 0) + (dy != 0) + (dx != 0);
+          if (nzero == 0 || (z + dz) < 0 || (z + dz) >= Z) continue;
+          const float w = nzero == 1 ? w1 : (nzero == 2 ? w2 : w3);
+          best = fminf(best, __fadd_rn(pl[dz + 1][cpos + dy * kRowF + dx], w));
+        }
+        best = fminf(best, 11.0f);
+      }
+      dst[((size_t)z * Y + y) * X + x] = best;
+    }
+    __syncthreads();
+    const int t = sm;
+    sm = sc;
+    sc = sp;
+    sp = t;
+  }
+}
+
+
 __global__ void __launch_bounds__(256) acwe_dist_init_kernel(const uint8_t* __restrict__ L, uint64_t n,
                                                              float* __restrict__ dist) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -772,6 +842,19 @@ extern "C" int si_acwe_dist_init(const uint8_t* L, uint64_t n, float* dist, void
   if (n == 0) return SI_OK;
   acwe_dist_init_kernel<<<grid_n(n, 256), 256, 0, as_stream(stream)>>>(L, n, dist);
   return check_launch("si_acwe_dist_init");
+}
+
+extern "C" int si_acwe_chamfer_band(float* dist, float* tmp, int Z, int Y, int X, void* stream) {
+  clear_error();
+  if (!dist || !tmp) return set_error(SI_ERR_ARG, "si_acwe_chamfer_band: null pointer");
+  if (!dims_ok(Z, Y, X) || dist == tmp) return set_error(SI_ERR_ARG, "si_acwe_chamfer_band: bad arguments");
+  cudaStream_t st = as_stream(stream);
+  const dim3 block(kTX, kTY);
+  const dim3 grid((X + kTX - 1) / kTX, (Y + kTY - 1) / kTY, (Z + kZChunk - 1) / kZChunk);
+  float* buf[2] = {dist, tmp};
+  for (int k = 0; k < 10; ++k)  // an even number of passes: the result is back in dist
+    acwe_chamfer_pass_kernel<<<grid, block, 0, st>>>(buf[k & 1], Z, Y, X, buf[(k + 1) & 1]);
+  return check_launch("si_acwe_chamfer_band");
 }
 
 extern "C" int si_acwe_refine_hist(const float* dist, const uint8_t* D, const uint8_t* L, const int16_t* class_lut,

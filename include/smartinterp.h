@@ -629,8 +629,8 @@ int si_nn_probs(const float* logits, int Ds, int H, int W, int zb, int ze,
  *   steps x (zero sums -> si_acwe_label_sums -> si_acwe_evolution ->
  *   si_acwe_curvop for every label) -> si_acwe_scatter.
  * Sequence, refined: si_acwe_minmax -> si_acwe_gather -> si_acwe_dist_init ->
- *   si_geo_scan(dist, zero image, lamb 0.0, 1 iteration) ->
- *   si_acwe_refine_hist -> si_acwe_refine_decide -> si_acwe_refine_apply. */
+ *   si_acwe_chamfer_band -> si_acwe_refine_hist -> si_acwe_refine_decide ->
+ *   si_acwe_refine_apply. */
 
 /* mm[0] = min, mm[1] = max (float32 values) of the voxels of an image array
  * that lie in the padded frame's interior; the array's voxel (a, b, c) is
@@ -686,6 +686,17 @@ int si_acwe_scatter(const uint8_t* L, int cz0, int cy0, int cx0, int cZ,
 
 /* dist[i] = 100 where L[i] == 0, else 0 (active_contour.py:206-207). */
 int si_acwe_dist_init(const uint8_t* L, uint64_t n, float* dist, void* stream);
+
+/* The refinement's chamfer distance (active_contour.py:45-81, one forward and
+ * one backward pass from si_acwe_dist_init's map) in the form the band test
+ * `distance <= 10` needs: 10 Jacobi passes of the 27-point min-plus stencil
+ * (weights 1, sqrt2, sqrt3; rows and columns 0 and n-1 keep their values;
+ * values clamped to 11). For every voxel that reaches the result this gives
+ * the same band as the reference's scan (the path lengths near 10 are
+ * exactly 10 or at least 0.0246 away from it). dist (Z x Y x X float32) is
+ * updated in place; tmp: scratch of the same size. */
+int si_acwe_chamfer_band(float* dist, float* tmp, int Z, int Y, int X,
+                         void* stream);
 
 /* Band histograms of the refinement: hist[z][class_lut[L]][D] counts the
  * crop voxels of slice z with dist <= 10 (active_contour.py:209-210,

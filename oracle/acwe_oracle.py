@@ -13,7 +13,8 @@ typing:
   * refinement's chamfer scan (active_contour.py:45-81) equals the geodesic
     raster scan with a zero image, lamb = 0 and one iteration (same 13
     neighbours and domain, cost c + d in binary64, binary32 store), so it is
-    computed by ``geo_oracle.raster_scan``.
+    computed by ``geo_oracle.raster_scan`` — the literal sequential scan, the
+    yardstick of the device's Jacobi band.
 The refinement's per-slice statistics use NumPy's mean, std and exp on the
 slice arrays exactly as the reference writes them.
 Pinned by tests/golden/ref_acwe.npz, made by the reference's own functions

@@ -101,6 +101,41 @@ def test_stencil_passes_bit_exact(shape, cuda):
             assert np.array_equal(Lc.cpu().numpy().reshape(shape), A.curvop(lab, steps, label)), (label, steps)
 
 
+@pytest.mark.parametrize("kind", ["points", "blobs"])
+@pytest.mark.parametrize("shape", [(12, 20, 40), (30, 25, 33), (6, 41, 70)], ids=["12x20x40", "30x25x33", "6x41x70"])
+def test_chamfer_band_equals_reference_scan(kind, shape, cuda):
+    """si_acwe_chamfer_band (Jacobi relaxation) against the reference's
+    forward/backward raster scan (the oracle's restatement): distance <= 10
+    agrees on every voxel off the crop's first and last planes, rows and
+    columns (where, in a real crop, padding or voxels 100 away from any
+    label sit), and those rows and columns are never band. Labels are kept
+    off that shell, as in a padded crop."""
+    rng = np.random.default_rng(sum(shape) + len(kind))
+    if kind == "points":
+        lab = (rng.random(shape) < 0.002).astype(np.uint8) * 3
+    else:
+        Z, Y, X = shape
+        _, blobs = blob_volume(shape, sum(shape), [1, 2], [(Z / 2, Y / 3, X / 2), (Z / 3, Y / 2, X / 4)],
+                               [(Z / 4, 6, 8), (2, 4, 3)], 5.0)
+        lab = blobs.astype(np.uint8)
+    lab[0] = lab[-1] = 0
+    lab[:, 0] = lab[:, -1] = 0
+    lab[:, :, 0] = lab[:, :, -1] = 0
+    assert lab.any()
+    _, band = A.chamfer_band(lab)
+    n = lab.size
+    L = torch.from_numpy(lab.ravel()).to(cuda)
+    d = torch.empty(n, dtype=torch.float32, device=cuda)
+    t = torch.empty_like(d)
+    nat.call("si_acwe_dist_init", L.data_ptr(), n, d.data_ptr(), _stream())
+    nat.call("si_acwe_chamfer_band", d.data_ptr(), t.data_ptr(), *shape, _stream())
+    got = d.cpu().numpy().reshape(shape) <= 10
+    core = (slice(1, -1),) * 3
+    assert np.array_equal(got[core], band[core]), int(np.count_nonzero(got[core] != band[core]))
+    assert not got[:, 0].any() and not got[:, -1].any() and not got[:, :, 0].any() and not got[:, :, -1].any()
+    assert 0 < band[core].mean() < 1  # the band neither empty nor everything
+
+
 RANDOM = [((12, 14, 16), np.uint8, 1.0, 1, 3), ((20, 30, 41), np.float32, 0.7, 2, 2), ((7, 9, 230), np.uint16, 1.0,
           0, 2), ((3, 40, 36), np.int16, 2.2, 3, 1), ((2, 6, 7), np.uint8, 1.0, 1, 2)]
 
