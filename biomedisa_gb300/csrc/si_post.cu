@@ -352,7 +352,14 @@ __global__ void __launch_bounds__(256, kP == 1 ? 3 : 2) smooth_tma_kernel(const 
         f2_unpack(num, na, nb);
         f2_unpack(den, da, db);
         f2_unpack(c_c[p], ca, cb);
-        const float ka = __fdiv_rn(na, da), kb = __fdiv_rn(nb, db);
+        // den >= 1e-10 > 0, so a zero numerator gives kappa = num (its sign
+        // kept) exactly; flat neighbourhoods (zero regions of a hit map) skip
+        // the division
+        float ka = na, kb = nb;
+        if (na != 0.0f || nb != 0.0f) {
+          ka = __fdiv_rn(na, da);
+          kb = __fdiv_rn(nb, db);
+        }
         float oa, ob;
         if (kF64) {
           oa = __double2float_rn(__dadd_rn((double)ca, __dmul_rn(0.01, (double)ka)));
