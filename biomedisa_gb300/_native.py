@@ -49,6 +49,7 @@ _SIGNATURES = {
     "si_walk_sorted_set_loop": [_c_int],
     "si_walk_sorted_set_round_limit": [_c_u64],
     "si_nn_umma_status": [_c_void_p, _c_void_p],
+    "si_nn_conv16_tc_set_streams": [_c_int],
     "si_nn_conv16_tc": [_c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int,
                         _c_int, _c_int, _c_void_p],
     "si_walk_bricks_scratch": [_c_int, _c_int, _c_int, _c_u64, _c_int, _c_void_p],

@@ -567,6 +567,13 @@ int si_nn_conv16_tc(const void* x, const void* w, const float* bias,
  * reference. */
 int si_nn_umma_status(int* status, void* stream);
 
+/* Interleaved column streams per CTA of si_nn_conv16_tc: 1 (default), 2 or
+ * 4. Each stream accumulates into its own tensor-memory ring, and the MMAs
+ * of a group alternate between streams, so consecutive MMAs accumulate into
+ * different columns (measured slower than one stream on GB300).
+ * Process-wide; results do not depend on it. */
+int si_nn_conv16_tc_set_streams(int streams);
+
 /* dw[27][cout][cin] += sum_v dy[v][co] x[v + off][ci]; db[cout] += sum_v dy
  * (db nullable). (cout, cin) in {16, 32}^2. With `partials` (cin = cout = 16
  * only; size from si_nn_wgrad_partial_bytes, 16-byte aligned) every block

@@ -63,12 +63,25 @@ def test_conv_forward_dgrad_wgrad(cin, cout, dil, shape, cuda):
 
 
 @pytest.mark.parametrize("dil,shape", [(1, (1, 3, 4, 300)), (2, (2, 5, 3, 257)), (8, (1, 4, 6, 128)),
-                                       (4, (3, 2, 2, 1))])
-def test_conv16_tensor_core_rows(dil, shape, cuda):
+                                       (4, (3, 2, 2, 1)), (1, (2, 4, 70, 130)), (2, (2, 40, 20, 200))])
+@pytest.mark.parametrize("streams", [1, 2, 4])
+def test_conv16_tensor_core_rows(dil, shape, streams, cuda):
     """The 16 -> 16 convolution on the tcgen05 tensor cores (si_nn_conv16_tc)
-    in tiles of 128 voxels of an x-row (several tiles per CTA, partial last
-    tiles, rows shorter than a tile): forward with bias, residual and ReLU, and
-    the data gradient, against the float64 oracle and the mma.sync path."""
+    in tiles of 128 voxels of an x-row (partial last tiles, rows shorter than
+    a tile, columns of 70 rows that wrap the accumulator rings of 30, 14 or 6
+    positions per stream and the 10-slot row ring, several columns per CTA):
+    forward with bias,
+    residual and ReLU, and the data gradient, against the float64 oracle and
+    the mma.sync path; with 1, 2 and 4 interleaved column streams per CTA."""
+    from biomedisa_gb300 import _native as nat
+    nat.call("si_nn_conv16_tc_set_streams", streams)
+    try:
+        _conv16_tc_case(dil, shape, cuda)
+    finally:
+        nat.call("si_nn_conv16_tc_set_streams", 1)
+
+
+def _conv16_tc_case(dil, shape, cuda):
     rng = np.random.default_rng(dil * 31 + shape[-1])
     x = NO.bf16_round(rng.standard_normal(shape + (16,)))
     c, w, b = _conv(16, 16, dil, rng, cuda)
