@@ -18,12 +18,13 @@
 // over all its columns (column c starts at k = P_c, P_{c+1} = P_c + nt + 2);
 // input k adds into ring positions k, k + 1, k + 2 and completes position k
 // (output j = k - P_c - 2 of its column; positions P_c and P_c + 1 are
-// padding). Positions live in 30 slots of 16 columns (k mod 30) of the 512
-// tensor-memory columns; a region starting at slot 28 or 29 runs on into
-// physical slots 30 and 31, which hold further partial sums of positions 0
-// and 1 (mod 30): the epilogue adds the two. Every MMA accumulates; the
-// epilogue zeroes a position's slots (tcgen05.st) after reading them and
-// before releasing them, and all slots start zeroed.
+// padding). Positions live in the 32 slots of 16 columns (k mod 32) of the
+// 512 tensor-memory columns; a region starting at slot 30 or 31 is issued as
+// two MMAs (N = 32 + 16 or 16 + 32) that continue at slot 0, so every
+// position sums its 27 products in one slot, in the same order wherever it
+// falls in the ring (results do not depend on the grid). Every MMA
+// accumulates; the epilogue zeroes a position's slot (tcgen05.st) after
+// reading it and before releasing it, and all slots start zeroed.
 //
 // Shared-memory operands, K-major without swizzle (core matrices of 8 rows x
 // 16 bytes): an input z-row is one TMA box of {8 channels, 128 + 2*dil
@@ -87,17 +88,20 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
   return d;                // base offset 0, absolute offsets, no swizzle
 }
 
-// kind::f16 instruction descriptor: fp32 D, bf16 A and B, both K-major, M = 128, N = 48.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(48 >> 3) << 17) |
-                            ((uint32_t)(kTileM >> 4) << 24);
+// kind::f16 instruction descriptor: fp32 D, bf16 A and B, both K-major, M = 128, N = kN.
+template <int kN>
+__host__ __device__ constexpr uint32_t idesc_f16() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) | ((uint32_t)(kTileM >> 4) << 24);
+}
 
 // Executed by a whole warp with warp-uniform operands (which then stay in
 // uniform registers); one elected lane issues the MMA / the commit.
+template <int kN>
 __device__ __forceinline__ void umma_f16(uint32_t d_tmem, uint64_t a, uint64_t b) {
   asm volatile(
       "{\n\t.reg .pred p, e;\n\tsetp.ne.b32 p, 1, 0;\n\telect.sync _|e, 0xffffffff;\n\t"
       "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(kIdesc)
+      "l"(a), "l"(b), "r"(idesc_f16<kN>())
       : "memory");
 }
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
@@ -206,9 +210,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv16_umma_kernel(const __grid_c
                                                                  const float* __restrict__ bias, int has_res,
                                                                  void* __restrict__ y_out, UmmaGeom g, int relu,
                                                                  uint32_t wait_lim) {
-  constexpr int kStreamSlots = 32 / kNS;  // physical 16-column slots of a stream
-  constexpr int kR = kStreamSlots - 2;    // its ring positions (the last two slots alias positions 0 and 1)
-  static_assert(kR >= 4, "accumulator ring too short");
+  constexpr int kR = 32 / kNS;  // ring positions (16-column slots) of a stream
+  static_assert(kR >= 8, "accumulator ring too short");
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
   uint8_t* sw = smem;                             // weight blocks [dz][dx][half][48][8]
@@ -264,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv16_umma_kernel(const __grid_c
   tmem_fence_after();
   const uint32_t tmem = tmem_base;
   const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;  // this warp's tensor-memory lane quadrant
-  if (warp >= 2 && warp < 6) {  // all 32 physical slots start at zero
+  if (warp >= 2 && warp < 6) {  // all 32 slots start at zero
     for (int b = 0; b < 32; ++b) tmem_zero16(tmem + lane_base + (uint32_t)(16 * b));
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
   }
@@ -382,9 +385,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv16_umma_kernel(const __grid_c
     // slot's base and the accumulator column change; a group's MMAs
     // alternate between its streams
     const uint32_t tm = __shfl_sync(0xffffffffu, tmem, 0);
-    uint64_t bdesc[9];
-#pragma unroll
-    for (int b = 0; b < 9; ++b) bdesc[b] = smem_desc(smem_u32(sw) + (uint32_t)(b * kWBlockBytes), 768, 128);
+    // weight block b = dz*3 + dx: descriptor bdesc0 + b * kWBlockBytes / 16
+    const uint64_t bdesc0 = smem_desc(smem_u32(sw), 768, 128);
     const uint64_t adesc0 = smem_desc(smem_u32(rows), 16u * (uint32_t)rv, 128);
     const uint64_t ddx = (uint64_t)dil;  // one dx step in descriptor start-address units (16 bytes)
     Ring<kRowSlots> rr;
@@ -409,7 +411,8 @@ __global__ void __launch_bounds__(kThreads, 1) conv16_umma_kernel(const __grid_c
       if (ns == 0) break;
       bool ok = true;
       uint64_t ad[kNS];
-      uint32_t dd[kNS], zm[kNS];
+      uint32_t dd[kNS], d0[kNS], zm[kNS];
+      int wrap[kNS];  // 0: the region fits; 1: 2 + 1 slots split at the ring end; 2: 1 + 2
       int slot[kNS];
       Ring<kRowSlots> r2 = rr;
 #pragma unroll
@@ -421,7 +424,9 @@ __global__ void __launch_bounds__(kThreads, 1) conv16_umma_kernel(const __grid_c
         ok = ok && mbar_wait_fast(&full_bar[r2.idx], r2.ph, wait_lim);
         if (w2[s]) ok = ok && mbar_wait_fast(&free_bar[s * kR + p2[s]], ph2[s] ^ 1u, wait_lim);
         ad[s] = adesc0 + (uint64_t)((r2.idx * kSlotBytes) >> 4);
-        dd[s] = tm + (uint32_t)(s * kStreamSlots * 16 + 16 * t.p);
+        dd[s] = tm + (uint32_t)(s * kR * 16 + 16 * t.p);
+        d0[s] = tm + (uint32_t)(s * kR * 16);
+        wrap[s] = t.p <= kR - 3 ? 0 : (t.p == kR - 2 ? 1 : 2);
         const int yy = row_y(t);
         if (yy >= 0 && yy < g.H)
 #pragma unroll
@@ -436,14 +441,42 @@ __global__ void __launch_bounds__(kThreads, 1) conv16_umma_kernel(const __grid_c
         break;
       }
       tmem_fence_after();
+      bool any_wrap = false;
 #pragma unroll
-      for (int dz = 0; dz < 3; ++dz)
+      for (int s = 0; s < kNS; ++s) any_wrap |= wrap[s] != 0;
+      if (!any_wrap) {  // every region fits: 9 MMAs of N = 48 per item
 #pragma unroll
-        for (int dx = 0; dx < 3; ++dx)
+        for (int dz = 0; dz < 3; ++dz)
 #pragma unroll
-          for (int s = 0; s < kNS; ++s)
-            if (zm[s] & (1u << dz))
-              umma_f16(dd[s], ad[s] + (uint64_t)((dz * kRowBytes) >> 4) + (uint64_t)dx * ddx, bdesc[dz * 3 + dx]);
+          for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+            for (int s = 0; s < kNS; ++s)
+              if (zm[s] & (1u << dz))
+                umma_f16<48>(dd[s], ad[s] + (uint64_t)((dz * kRowBytes) >> 4) + (uint64_t)dx * ddx,
+                             bdesc0 + (uint64_t)((dz * 3 + dx) * (kWBlockBytes >> 4)));
+      } else {
+#pragma unroll 1
+        for (int dz = 0; dz < 3; ++dz)
+#pragma unroll 1
+          for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+            for (int s = 0; s < kNS; ++s) {
+              if (!(zm[s] & (1u << dz))) continue;
+              const uint64_t a = ad[s] + (uint64_t)((dz * kRowBytes) >> 4) + (uint64_t)dx * ddx;
+              const uint64_t b = bdesc0 + (uint64_t)((dz * 3 + dx) * (kWBlockBytes >> 4));
+              // a region running past the ring end continues at slot 0; the
+              // second piece starts 32 or 16 weight rows (16 bytes each) in
+              if (wrap[s] == 0) {
+                umma_f16<48>(dd[s], a, b);
+              } else if (wrap[s] == 1) {
+                umma_f16<32>(dd[s], a, b);
+                umma_f16<16>(d0[s], a, b + 32);
+              } else {
+                umma_f16<16>(dd[s], a, b);
+                umma_f16<32>(d0[s], a, b + 16);
+              }
+            }
+      }
 #pragma unroll
       for (int s = 0; s < kNS; ++s) {
         if (!live[s]) continue;
@@ -492,22 +525,14 @@ __global__ void __launch_bounds__(kThreads, 1) conv16_umma_kernel(const __grid_c
           continue;
         }
         tmem_fence_after();
-        const uint32_t ta = tmem + lane_base + (uint32_t)(s * kStreamSlots * 16 + 16 * p);
+        const uint32_t ta = tmem + lane_base + (uint32_t)(s * kR * 16 + 16 * p);
         if (t.i >= 2) {  // output row j = i - 2 of the column
           uint32_t v[16];
           tmem_ld16(ta, v);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
           float u[16];
-          if (p < 2) {
-            uint32_t v2[16];
-            tmem_ld16(ta + 16u * kR, v2);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int e = 0; e < 16; ++e) u[e] = __uint_as_float(v[e]) + __uint_as_float(v2[e]);
-          } else {
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int e = 0; e < 16; ++e) u[e] = __uint_as_float(v[e]);
-          }
+          for (int e = 0; e < 16; ++e) u[e] = __uint_as_float(v[e]);
           const int x = t.c.x0 + m, yo = t.c.yph + (t.i - 2) * dil;
           if (x < g.W) {
             const long long r = (((long long)t.c.n * g.D + t.c.z) * g.H + yo) * g.W + x;
@@ -548,7 +573,6 @@ __global__ void __launch_bounds__(kThreads, 1) conv16_umma_kernel(const __grid_c
           }
         }
         tmem_zero16(ta);
-        if (p < 2) tmem_zero16(ta + 16u * kR);
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         tmem_fence_before();
         __syncwarp();

@@ -138,12 +138,14 @@ def relu_bwd(g, y, add=None):
 class SurrogateNet:
     """The network; parameters live on the current CUDA device."""
 
-    def __init__(self, channels=16, dilations=(1, 2, 4, 8), seed=0, device=None, tensor_core=False):
+    def __init__(self, channels=16, dilations=(1, 2, 4, 8), seed=0, device=None, tensor_core=True):
         if channels not in (16, 32):
             raise ValueError("channels must be 16 or 32")
         self.device = torch.device(device) if device else torch.device("cuda", torch.cuda.current_device())
         self.channels, self.dilations = channels, tuple(dilations)
-        self.tensor_core = bool(tensor_core)  # 16 -> 16 layers on the tcgen05 kernel
+        # 16 -> 16 layers (forward and data gradient) on the tcgen05 kernel;
+        # False: on mma.sync
+        self.tensor_core = bool(tensor_core)
         g = torch.Generator(device="cpu").manual_seed(seed)
         self.convs = [self._make(IN_CH, channels, 1, g)]
         for d in self.dilations:

@@ -68,7 +68,7 @@ def test_conv_forward_dgrad_wgrad(cin, cout, dil, shape, cuda):
 def test_conv16_tensor_core_rows(dil, shape, streams, cuda):
     """The 16 -> 16 convolution on the tcgen05 tensor cores (si_nn_conv16_tc)
     in tiles of 128 voxels of an x-row (partial last tiles, rows shorter than
-    a tile, columns of 70 rows that wrap the accumulator rings of 30, 14 or 6
+    a tile, columns of 70 rows that wrap the accumulator rings of 32, 16 or 8
     positions per stream and the 10-slot row ring, several columns per CTA):
     forward with bias,
     residual and ReLU, and the data gradient, against the float64 oracle and
