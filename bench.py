@@ -11,7 +11,9 @@ labelling of the reference's published timing case), large (1024^3), large_ref
 (1024^3 with the reference large path's seed set), batch (32 uneven uint16
 volumes in one batched walk), train (surrogate training voxels/s), hybrid
 (surrogate + restricted walk vs the plain walk at 1024^3, voxels/s), geodesic
-(geodesic raster-scan interpolation of the plain volume, voxels/s).
+(geodesic raster-scan interpolation of the plain volume, voxels/s), acwe (the
+active-contour post-processing, voxels/s), conv16 (the surrogate's 16->16
+convolution on the tensor cores alone, voxels/s).
 
 Metric: walker-steps/s = (seeds * nbrw * sorw) / step time (whole job).
 ``e2e`` is the same metric through ``smart_interpolation`` with numpy inputs
@@ -20,7 +22,7 @@ and outputs (host->device copies and result download inside the timed region).
 ``--impl reference`` times the reference's own CPU walker on the host cores.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                       [--workload allaxis|plain|screw|batch|large|large_ref|train|hybrid|geodesic]
+                       [--workload allaxis|plain|screw|batch|large|large_ref|train|hybrid|geodesic|acwe|conv16]
 """
 from __future__ import annotations
 
@@ -65,6 +67,10 @@ WORKLOADS = {
                        "bf16 activations/weights with fp32 accumulation, batch 8 windows of 64^3 from 16 walked "
                        "128^3 volumes (procedural and large-style), soft-target cross entropy, AdamW",
                   nbrw=10, sorw=4000, smooth=0, allaxis=False),
+    "conv16": dict(desc="the surrogate's 16->16 3x3x3 convolution (dilation 1, bias, residual and ReLU, bf16 in "
+                        "and out, fp32 accumulation) of a (n,z,y,x) = (1,128,256,1024) bf16 volume (1 GiB per "
+                        "activation) on the tcgen05 kernel; the mma.sync kernel timed beside it on the same input",
+                   nbrw=0, sorw=0, smooth=0, allaxis=False),
     "hybrid": dict(desc="hybrid vs plain on the large uint8 1024^3 volume (6 phases, labels every 12th z-slice, "
                         "nbrw=10, sorw=4000, smooth=100 in both arms): surrogate everywhere, walk from the seeds "
                         "within 8 voxels of voxels with max p < 0.9 (grown by 2), then 100 smoothing iterations; "
@@ -347,6 +353,9 @@ def main():
         return
     if args.workload in ("hybrid", "hybrid_097"):
         run_hybrid_bench(args, wl)
+        return
+    if args.workload == "conv16":
+        run_conv16_bench(args, wl)
         return
     if args.workload == "geodesic":
         run_geodesic_bench(args, wl)
@@ -673,11 +682,11 @@ def run_train_bench(args, wl):
     c = net.convs[1]
     shape = (batch, patch, patch, patch)
     for _ in range(3):
-        SG.conv_fwd(x, c, shape, relu=True)
+        SG.conv_fwd(x, c, shape, relu=True, tensor_core=net.tensor_core)
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s.record(stream)
     for _ in range(20):
-        SG.conv_fwd(x, c, shape, relu=True)
+        SG.conv_fwd(x, c, shape, relu=True, tensor_core=net.tensor_core)
     e.record(stream)
     torch.cuda.synchronize()
     conv_ms = s.elapsed_time(e) / 20
@@ -707,12 +716,117 @@ def run_train_bench(args, wl):
         "gpu_launches": launches,
         "roofline": {"bound": "tensor", "achieved": conv_tflops, "peak": bf16, "unit": "TFLOP/s",
                      "frac": conv_tflops / bf16, "traffic": None,
-                     "note": f"16->16 forward convolution (conv16_kernel, mma.sync bf16), 2*27*16*16 FLOP per "
-                             f"output voxel x {vox} voxels / CUDA-event time; peak {kind} bf16 (cuBLAS burst)"},
+                     "note": f"16->16 forward convolution ({'conv16_umma_kernel, tcgen05' if net.tensor_core else 'conv16_kernel, mma.sync'} "
+                             f"bf16), 2*27*16*16 FLOP per output voxel x {vox} voxels / CUDA-event time; peak "
+                             f"{kind} bf16 (cuBLAS burst)"},
         "clocks": clocks.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = nn_cpu_baseline(net, min(args.ref_seconds, 20.0))
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def run_conv16_bench(args, wl):
+    """The surrogate's 16->16 convolution alone: one step = one forward
+    convolution on the tensor cores (si_nn_conv16_tc) of a (1,128,256,1024)
+    bf16 volume with bias, residual and ReLU; the mma.sync kernel is timed on
+    the same input beside it, and ``e2e`` runs the same call on pinned host
+    arrays (input and residual in, output out)."""
+    import torch
+
+    from biomedisa_gb300 import _native as nat
+    from biomedisa_gb300 import surrogate as SG
+
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned surrogate and no "
+                              "convolution"}))
+        return
+    world, rank, local = dist_setup()
+    shape = (1, 128, 256, 1024)
+    vox = shape[0] * shape[1] * shape[2] * shape[3]
+    net = SG.SurrogateNet(seed=0)
+    c = net.convs[1]
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    x = (torch.randn(shape + (16,), device="cuda", generator=gen) * 0.5).to(torch.bfloat16)
+    res = (torch.randn(shape + (16,), device="cuda", generator=gen) * 0.5).to(torch.bfloat16)
+
+    def conv(xi, ri, tc=True):
+        return SG.conv_fwd(xi, c, shape, relu=True, residual=ri, tensor_core=tc)
+
+    for _ in range(args.warmup):
+        conv(x, res)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    l2buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    times, launches = [], 0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush_l2(l2buf)
+            torch.cuda.synchronize()
+            barrier(world)
+            before = dict(nat.CALLS)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            y = conv(x, res)
+            e.record(stream)
+            torch.cuda.synchronize()
+            barrier(world)
+            times.append(s.elapsed_time(e))
+            launches = launches_since(before)
+    SG.umma_check()
+    ms = max_over_ranks(world, sum(times) / len(times))
+    flops = 2 * 27 * 16 * 16 * vox
+    tflops = flops / (ms / 1e3) / 1e12
+    mma_t = []
+    for _ in range(max(3, args.steps)):
+        flush_l2(l2buf)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        ym = conv(x, res, tc=False)
+        e.record(stream)
+        torch.cuda.synchronize()
+        mma_t.append(s.elapsed_time(e))
+    mma_ms = sum(mma_t) / len(mma_t)
+    diff = float((ym.float() - y.float()).abs().max())
+    xh, rh = x.cpu().pin_memory(), res.cpu().pin_memory()
+    yh = torch.empty(shape + (16,), dtype=torch.bfloat16).pin_memory()
+    e2e_t = []
+    for _ in range(args.e2e_steps or args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        yd = conv(xh.to("cuda", non_blocking=True), rh.to("cuda", non_blocking=True))
+        yh.copy_(yd, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    SG.umma_check()
+    e2e_s = max_over_ranks(world, sum(e2e_t) / len(e2e_t))
+    act = vox * 16 * 2
+    pk = peaks()
+    bf16 = float(pk.get("bf16_tflops", 1900.0))
+    kind = "measured" if "bf16_tflops" in pk else "fallback"
+    hbm = float(pk.get("hbm_gbs", 6800.0))
+    line = {
+        "metric": "voxels/s", "value": world * vox / (ms / 1e3), "unit": "voxels/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16", "data": "synthetic (seeded normal activations, the network's own "
+        "initial weights)",
+        "config": {"workload": wl["desc"], "global_batch": 1, "parallelism": "single GPU",
+                   "l2": "256 MiB buffer written before every timed step; activations 1 GiB > L2"},
+        "mma_sync_ms": mma_ms, "speedup_vs_mma_sync": mma_ms / ms, "max_abs_diff_vs_mma_sync": diff,
+        "e2e": {"value": world * vox / e2e_s, "unit": "voxels/s", "seconds": e2e_s, "h2d_bytes_per_step": 2 * act,
+                "d2h_bytes_per_step": act,
+                "note": "the same call on pinned host arrays: input and residual copied in, output copied out"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "tensor", "achieved": tflops, "peak": bf16, "unit": "TFLOP/s", "frac": tflops / bf16,
+                     "traffic": None,
+                     "hbm_frac": 3 * act / (ms / 1e3) / 1e9 / hbm,
+                     "note": f"conv16_umma_kernel: 2*27*16*16 FLOP per output voxel x {vox} voxels / CUDA-event "
+                             f"time; peak {kind} bf16 (cuBLAS burst); hbm_frac = (input + residual + output, "
+                             f"96 B per voxel) / time over the {kind} HBM copy bandwidth"},
+        "clocks": clocks.summary(),
+    }
     if rank == 0:
         print(json.dumps(line))
 
