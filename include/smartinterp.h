@@ -548,13 +548,13 @@ int si_nn_conv3d_fwd(const void* x, const void* w, const float* bias,
 
 /* The 16 -> 16 convolution of si_nn_conv3d_fwd (same arguments without
  * cin/cout; dil <= 8; 16-byte aligned tensors) on the 5th-generation tensor
- * cores: tcgen05.mma (M = 128 voxels of an x-row, N = 16 output channels,
- * K = 16 input channels per tap, fp32 accumulators in tensor memory) over
- * input rows staged by TMA, one MMA per tap. Same results as
- * si_nn_conv3d_fwd up to fp32 accumulation order. Selectable through
- * SurrogateNet(tensor_core=True); on this network's 16-channel layers it is
- * slower than the mma.sync path (measured), so that one is the default. No
- * counterpart in the reference. */
+ * cores, organised by input rows: per input row and (dz, dx) one tcgen05.mma
+ * of M = 128 voxels of an x-row, N = 48 (the three output rows the input row
+ * meets, 16 channels each), K = 16, into a ring of fp32 accumulators in
+ * tensor memory; rows staged by TMA. Same results as si_nn_conv3d_fwd up to
+ * fp32 accumulation order, and independent of the grid. The default of
+ * SurrogateNet for its 16 -> 16 layers (2.4x the mma.sync kernel on large
+ * volumes, measured). No counterpart in the reference. */
 int si_nn_conv16_tc(const void* x, const void* w, const float* bias,
                     const void* residual, void* y, int N, int D, int H, int W,
                     int dil, int relu, int out_f32, void* stream);
