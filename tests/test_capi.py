@@ -44,6 +44,24 @@ def test_argument_errors_without_launch(native_lib):
     assert _native.SI_F32 == 5
 
 
+def test_conv16_tc_argument_errors_without_launch(native_lib):
+    """The tensor-core convolution rejects a bad stream count, dilation or
+    shape before any CUDA call."""
+    import ctypes
+
+    assert native_lib.si_nn_conv16_tc_set_streams(3) == 1
+    assert b"1, 2 or 4" in native_lib.si_last_error()
+    assert native_lib.si_nn_conv16_tc_set_streams(1) == 0
+    p = [ctypes.c_void_p(16 * (i + 1)) for i in range(4)]  # aligned, never dereferenced
+    for dil in (0, 9):
+        rc = native_lib.si_nn_conv16_tc(p[0], p[1], None, p[2], p[3], 1, 4, 4, 4, dil, 0, 0, None)
+        assert rc == 1 and b"dilation" in native_lib.si_last_error()
+    rc = native_lib.si_nn_conv16_tc(p[0], p[1], None, p[2], p[3], 0, 4, 4, 4, 1, 0, 0, None)
+    assert rc == 1 and b"bad shape" in native_lib.si_last_error()
+    rc = native_lib.si_nn_conv16_tc(ctypes.c_void_p(8), p[1], None, None, p[3], 1, 4, 4, 4, 1, 0, 0, None)
+    assert rc == 1 and b"16-byte aligned" in native_lib.si_last_error()
+
+
 def declared_arities():
     """Parameter count of every si_* declaration in the header."""
     text = (ROOT / "include" / "smartinterp.h").read_text()
