@@ -36,17 +36,21 @@
 // nor multiplied (their contribution is zero). The weights sit once per CTA
 // as 9 blocks [dz][dx] of [half][48][8 ci].
 //
-// Roles (one persistent CTA per SM, 10 warps): warp 0 issues the copies into
-// a ring of 10 input-row slots and, for a residual layer, each output row's
-// residual tile into a ring of 12 slots (so the epilogue never waits on a
-// global load); warp 1 issues the MMAs and two commits per input row (row
-// slot free; ring position complete), the whole warp running the loop with
-// warp-uniform operands and one elected lane issuing; two groups of four warps (2-5, 6-9)
-// run the epilogue of alternate items (thread m = tensor-memory lane m =
-// voxel x0 + m): bias, residual, ReLU, bf16 or fp32 store, zeroing, release. Every wait is bounded: a role
-// that gives up flags the CTA, the others stop at their next wait, the
-// copies and MMAs in flight are waited for (bounded), the tensor memory is
-// freed and the status records the error.
+// Roles (one persistent CTA per SM, 11 warps): warp 0 loads each input row's
+// z-rows into a ring of 10 row slots; warp 10 loads, for a residual layer,
+// each output row's residual tile into a ring of 12 slots (so the epilogue
+// never waits on a global load); warp 1 issues the 9 MMAs and two commits
+// per input row (row slot free; ring position complete); two groups of four
+// warps (2-5, 6-9) run the epilogue of alternate positions (thread m =
+// tensor-memory lane m = voxel x0 + m): bias, residual, ReLU, bf16 or fp32
+// store, zeroing, release. Warps 0, 1 and 10 run their loops as whole warps
+// with warp-uniform operands and issue from one elected lane (from a single
+// lane every MMA cost about 80 cycles of issue, measured). Optionally the
+// CTA's columns are dealt to 2 or 4 interleaved streams with rings of their
+// own (si_nn_conv16_tc_set_streams; measured slower than one). Every wait is
+// bounded: a role that gives up flags the CTA, the others stop at their next
+// wait, the copies and MMAs in flight are waited for (bounded), the tensor
+// memory is freed and the status records the error.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
