@@ -4,11 +4,11 @@ walker kernels and its own random stream, on benchmark configurations.
 The reference's smart_interpolation (Python host code unmodified, its CUDA
 kernel sources compiled for the CPU by oracle/ref_extract.py, pycuda and
 mpi4py faked by oracle/ref_run.py) is run on
-  * ``c1``: the plain single-volume configuration in full — uint8 128^3,
+  * ``plain128``: the plain single-volume configuration in full — uint8 128^3,
     background mean 60 plus two ellipsoids (means 130 and 200, semi-axes
     U[15, 45]), N(0, 15) noise, labels 0..2 on every 10th z-slice,
     nbrw=10, sorw=4000, smooth=0 (``synthetic.plain_volume(seed=0)``);
-  * ``c1_allaxis``: the same volume labelled on all three axes (every 10th
+  * ``plain128_allaxis``: the same volume labelled on all three axes (every 10th
     z-slice, every 16th y- and x-slice), allaxis=True, nbrw=10, sorw=4000,
     smooth=20;
   * ``slab``: a reduced slab of the all-axis configuration — uint8
@@ -46,8 +46,8 @@ import ref_run  # noqa: E402
 
 from biomedisa_gb300.synthetic import allaxis_volume, plain_volume, sparse_labels  # noqa: E402
 
-C1 = dict(nbrw=10, sorw=4000, smooth=0, allaxis=False)
-C1_ALLAXIS = dict(nbrw=10, sorw=4000, smooth=20, allaxis=True)
+PLAIN_128 = dict(nbrw=10, sorw=4000, smooth=0, allaxis=False)
+PLAIN_128_ALLAXIS = dict(nbrw=10, sorw=4000, smooth=20, allaxis=True)
 SLAB_SHAPE = (96, 128, 128)
 SLAB = dict(nbrw=10, sorw=4000, smooth=100, allaxis=True)
 
@@ -58,8 +58,8 @@ def digest(a: np.ndarray) -> str:
 
 def cases():
     img, lab, truth = plain_volume(seed=0)
-    yield "c1", img, lab, C1
-    yield "c1_allaxis", img, sparse_labels(truth.astype(np.int32), z_every=10, y_every=16, x_every=16), C1_ALLAXIS
+    yield "plain128", img, lab, PLAIN_128
+    yield "plain128_allaxis", img, sparse_labels(truth.astype(np.int32), z_every=10, y_every=16, x_every=16), PLAIN_128_ALLAXIS
     img, lab, _ = allaxis_volume(seed=0, shape=SLAB_SHAPE)
     yield "slab", img, lab, SLAB
 

@@ -53,10 +53,10 @@ def dice_per_label(a, b):
 
 
 def _inputs(name):
-    if name == "c1":
+    if name == "plain128":
         img, lab, _ = plain_volume(seed=0)
         return img, lab, dict(nbrw=10, sorw=4000, smooth=0, allaxis=False)
-    if name == "c1_allaxis":
+    if name == "plain128_allaxis":
         img, _, truth = plain_volume(seed=0)
         lab = sparse_labels(truth.astype(np.int32), z_every=10, y_every=16, x_every=16)
         return img, lab, dict(nbrw=10, sorw=4000, smooth=20, allaxis=True)
@@ -81,7 +81,7 @@ def _gate(name, ref, got, kw, what):
         assert min(d.values()) >= DICE_MIN, (name, key, d)
 
 
-@pytest.mark.parametrize("name", ["c1", "c1_allaxis"])
+@pytest.mark.parametrize("name", ["plain128", "plain128_allaxis"])
 def test_dice_against_reference_kernels(name, cuda):
     """The default product (Philox stream) against the reference's own
     kernels and stream: per-label Dice >= 0.99."""
@@ -89,7 +89,7 @@ def test_dice_against_reference_kernels(name, cuda):
     _gate(name, ref, smart_interpolation(img, lab, **kw), kw, "Philox")
 
 
-@pytest.mark.parametrize("name", ["c1", "c1_allaxis", "slab"])
+@pytest.mark.parametrize("name", ["plain128", "plain128_allaxis", "slab"])
 def test_reference_stream_dice_against_reference_kernels(name, cuda):
     """rng='reference' (the reference walker's own binary32 MRG stream) gives
     the reference's labels at per-label Dice >= 0.99 on every configuration,
