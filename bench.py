@@ -632,6 +632,32 @@ def nn_cpu_baseline(net, target_seconds=10.0):
                       f"(oracle/nn_oracle.py network_grads), {secs:.1f} s"}
 
 
+def conv_cpu_baseline(c, target_seconds=10.0):
+    """The float64 NumPy oracle's 16->16 convolution (bias, residual, ReLU)
+    of the same layer on a (1, 16, 32, 128) window, repeated for about
+    target_seconds (1 core)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import nn_oracle as NO
+
+    rng = np.random.default_rng(0)
+    shape = (1, 16, 32, 128)
+    x = NO.bf16_round(rng.standard_normal(shape + (16,)) * 0.5)
+    res = NO.bf16_round(rng.standard_normal(shape + (16,)) * 0.5)
+    w = c.w.cpu().numpy().astype(np.float64)
+    b = c.b.cpu().numpy().astype(np.float64)
+    vox = int(np.prod(shape))
+    t0, reps = time.perf_counter(), 0
+    while True:
+        np.maximum(NO.conv_fwd(x, w, b, c.dil) + res, 0)
+        reps += 1
+        if time.perf_counter() - t0 >= target_seconds:
+            break
+    secs = time.perf_counter() - t0
+    return {"value": reps * vox / secs, "unit": "voxels/s", "cores": 1, "kind": "port",
+            "sample": f"{reps} convolutions of a (1,16,32,128) window through the float64 NumPy oracle "
+                      f"(oracle/nn_oracle.py conv_fwd + residual + ReLU), {secs:.1f} s"}
+
+
 def run_train_bench(args, wl):
     """Surrogate training throughput: one step = forward, backward and AdamW
     over a batch of 8 windows of 64^3 (device-resident training set)."""
@@ -827,6 +853,8 @@ def run_conv16_bench(args, wl):
                              f"96 B per voxel) / time over the {kind} HBM copy bandwidth"},
         "clocks": clocks.summary(),
     }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = conv_cpu_baseline(c, min(args.ref_seconds, 10.0))
     if rank == 0:
         print(json.dumps(line))
 
